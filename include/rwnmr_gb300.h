@@ -1,0 +1,150 @@
+/* rwnmr_gb300 -- GB300-native random-walk NMR walker engine, C ABI.
+ *
+ * Drop-in boundary for the walker hot path of RandomWalk_NMR. The reference has no FFI of its
+ * own: its walks sit behind three C++ dispatch points, which these entry points replace:
+ *   NMR_Simulation::mapSimulation()   (NMR_Simulation/NMR_Simulation.h:264-267,
+ *                                      NMR_Simulation.cpp:1522-1539)  -> rwnmr_map_run
+ *   NMR_cpmg::run_simulation()        (NMR_Simulation/NMR_cpmg.cpp:149-175;
+ *                                      image_simulation_cuda/_omp)     -> rwnmr_cpmg_run
+ *   NMR_PFGSE::simulation()           (NMR_Simulation/NMR_pfgse.cpp:593-603;
+ *                                      simulation_cuda/_omp)           -> rwnmr_pfgse_run
+ * The host-side setup those methods read (NMR_Simulation::bitBlock, walkers[].initialPosition /
+ * initialSeed / decreaseFactor; NMR_Simulation.cpp:619-633, 1139-1333) is passed in through
+ * rwnmr_image_upload and rwnmr_walkers_upload.
+ *
+ * Conventions
+ *  - Every call returns an rwnmr_status; on failure rwnmr_last_error() describes it. The
+ *    reference prints and exit(1)s instead and checks no CUDA errors.
+ *  - Host pointers are caller-owned and only read or written during the call. The context owns
+ *    all device memory. No call resets the device (the reference's cudaDeviceReset() is not
+ *    reproduced: it would tear down other users of the same CUDA context).
+ *  - One context per host thread; calls on one context are serialised on its CUDA stream.
+ *  - There is no CPU fallback: without a usable CUDA device rwnmr_ctx_create fails.
+ */
+#ifndef RWNMR_GB300_H
+#define RWNMR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rwnmr_status
+{
+    RWNMR_OK = 0,
+    RWNMR_ERR_INVALID = 1,     /* bad argument or size */
+    RWNMR_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    RWNMR_ERR_NOMEM = 3,       /* device allocation failed */
+    RWNMR_ERR_STATE = 4,       /* call out of order (e.g. no image uploaded) */
+    RWNMR_ERR_UNSUPPORTED = 5, /* valid request this build does not handle */
+    RWNMR_ERR_DEVICE = 6       /* the kernel reported a fault through its status word */
+} rwnmr_status;
+
+/* Boundary conditions (rwnmr.config BC; ConfigFiles/rwnmr_config.cpp:228-240). */
+enum
+{
+    RWNMR_BC_NOFLUX = 0,
+    RWNMR_BC_PERIODIC = 1,
+    RWNMR_BC_MIRROR = 2
+};
+
+typedef struct rwnmr_ctx rwnmr_ctx;
+
+/* ---- context --------------------------------------------------------------------------- */
+rwnmr_status rwnmr_ctx_create(rwnmr_ctx **out, int device);
+void rwnmr_ctx_destroy(rwnmr_ctx *ctx);
+const char *rwnmr_last_error(const rwnmr_ctx *ctx);
+const char *rwnmr_version(void);
+/* Runs subsequent work on an external cudaStream_t (NULL restores the context's own stream). */
+rwnmr_status rwnmr_ctx_set_stream(rwnmr_ctx *ctx, void *cuda_stream);
+/* Kernels launched by this context so far (for launch accounting). */
+int64_t rwnmr_ctx_launch_count(const rwnmr_ctx *ctx);
+/* Device-side duration of the last walk kernel(s) of the last run call, in milliseconds. */
+double rwnmr_ctx_last_kernel_ms(const rwnmr_ctx *ctx);
+
+/* ---- image ----------------------------------------------------------------------------- */
+/* Bit-block image (BitBlock/bitBlock.cpp:138-221): blocks[bx + by*bcols + bz*bcols*brows],
+ * bit (x%4) + 4*(y%4) + 16*(z%4) set for solid voxels, bcols = ceil(nx/4) etc.
+ * labels (nullable): uint8 [nz][ny][nx], 0 = pore, p = solid of material phase p (1..n_phases);
+ * must agree with blocks. Multi-phase labels extend the reference (its image is binary). */
+rwnmr_status rwnmr_image_upload(rwnmr_ctx *ctx, const uint64_t *blocks, int32_t nx, int32_t ny, int32_t nz,
+                                const uint8_t *labels, int32_t n_phases);
+/* Same from a label volume alone; the bit-blocks are packed on the GPU. */
+rwnmr_status rwnmr_image_upload_labels(rwnmr_ctx *ctx, const uint8_t *labels, int32_t nx, int32_t ny, int32_t nz,
+                                       int32_t n_phases);
+/* Reads back the packed bit-blocks (ceil(nx/4)*ceil(ny/4)*ceil(nz/4) words). */
+rwnmr_status rwnmr_image_download_blocks(rwnmr_ctx *ctx, uint64_t *blocks);
+
+/* ---- walkers --------------------------------------------------------------------------- */
+/* Initial state (Walker::initialPosition / initialSeed). Positions are in walk units (voxels
+ * << voxel-division shift). */
+rwnmr_status rwnmr_walkers_upload(rwnmr_ctx *ctx, int64_t n, const int32_t *x0, const int32_t *y0, const int32_t *z0,
+                                  const uint64_t *seed0);
+/* State after the last run: positions, current RNG state, per-phase collision totals
+ * ([n][n_phases]). Any pointer may be NULL. */
+rwnmr_status rwnmr_walkers_download(rwnmr_ctx *ctx, int32_t *x, int32_t *y, int32_t *z, uint64_t *seed,
+                                    uint32_t *collisions);
+
+/* ---- CPMG walk ------------------------------------------------------------------------- */
+typedef struct rwnmr_cpmg_params
+{
+    int32_t bc;             /* RWNMR_BC_* */
+    int32_t shift;          /* log2(voxel division) */
+    int32_t steps_per_echo; /* STEPS_PER_ECHO */
+    int32_t n_echoes;       /* NMR_Simulation::numberOfEchoes */
+    const double *dfactor;  /* [n_phases] collision decrease factor per phase,
+                               1 - (2/3) rho res / (D0 1e3)  (Walker/walker.h:203-209) */
+    int32_t echoes_per_launch; /* 0 = automatic; bounds one kernel's duration */
+} rwnmr_cpmg_params;
+
+/* Walks every walker from its initial state for n_echoes * steps_per_echo steps
+ * (NMR_cpmg::image_simulation_cuda, NMR_cpmg_cuda.cpp:929-1774). Outputs (each nullable):
+ *   echo_sum  [n_echoes+1]    sum over walkers of the energy after each echo (index 0 =
+ *                             initial), un-normalised and without bulk relaxation, like the
+ *                             reference's signal_amps before applyBulk/normalizeSignal
+ *   echo_fx   [(n_echoes+1)*3] the same sums as exact fixed-point integers: each walker's
+ *                             energy is rounded to a multiple of 2^-63 and split into bits
+ *                             0-20, 21-41, 42-63, and each limb is summed over walkers
+ *   echo_coll [n_echoes*n_phases] collisions gained during each echo, per phase */
+rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, double *echo_sum, uint64_t *echo_fx,
+                            uint64_t *echo_coll);
+
+/* Vector-Jacobian product of rwnmr_cpmg_run by replaying every trajectory from its stored seed:
+ * grad_dfactor[p] = sum_e grad_echo[e] * d echo_sum[e] / d dfactor[p]. grad_echo: [n_echoes+1]. */
+rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, const double *grad_echo,
+                                double *grad_dfactor);
+
+/* ---- collision-mapping walk ------------------------------------------------------------ */
+/* NMR_Simulation::mapSimulation (NMR_Simulation.cpp:1787-1841; NMR_Simulation_cuda.cpp:726-1270):
+ * walks every walker from its initial state for `steps` steps and writes its collision count. */
+rwnmr_status rwnmr_map_run(rwnmr_ctx *ctx, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions);
+
+/* ---- PFGSE walk ------------------------------------------------------------------------ */
+typedef struct rwnmr_pfgse_params
+{
+    int32_t bc;
+    int32_t shift;
+    int32_t n_delta;      /* exposure times */
+    const int32_t *steps; /* [n_delta] walk steps to each exposure time, non-decreasing */
+    int32_t n_g;          /* gradient points */
+    const double *kvec;   /* [n_g][3] wave vectors k (1/um), NMR_pfgse.cpp:299-313,483-486 */
+    double res;           /* voxel resolution of the walk grid (um) */
+    const double *dfactor;/* [n_phases] */
+} rwnmr_pfgse_params;
+
+/* PFGSE walk (NMR_PFGSE::simulation_cuda/_omp): walkers walk cumulatively to each exposure time;
+ * then M[i][j] = sum_w E_w cos((k_j . dR_w) res), esum[i] = sum_w E_w (the reference normalises
+ * M by esum, NMR_pfgse.cpp:1795-1798), msd[i][a] = sum_w dR_a^2 (exact integer, walk units).
+ * Each output nullable. */
+rwnmr_status rwnmr_pfgse_run(rwnmr_ctx *ctx, const rwnmr_pfgse_params *p, double *M, double *esum, uint64_t *msd);
+
+/* d M[i][j] / d g_j for a gradient ramp g_j with k_j = kscale * g_j * dir (kscale = dk/dg,
+ * dir the unit gradient direction): dMdg[i][j] = -sum_w E_w sin((k_j . dR) res) (kscale dir . dR) res. */
+rwnmr_status rwnmr_pfgse_grad_g(rwnmr_ctx *ctx, const rwnmr_pfgse_params *p, double kscale, const double *dir,
+                                double *dMdg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,50 @@
+/* rwnmr_gb300 host frontend, C ABI: synthetic images, bit-block packing, walker placement,
+ * configuration files and the CPMG / PFGSE sequences that drive the GPU engine
+ * (include/rwnmr_gb300.h). Host-only code; no function here launches GPU work except the
+ * sequence drivers, which call the engine.
+ */
+#ifndef RWNMR_HOST_H
+#define RWNMR_HOST_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Overlapping-sphere pore image (the synthetic stand-in for micro-CT images): labels
+ * [nz][ny][nx] start as pore (0); solid spheres with uniform centres and radii uniform in
+ * [rmin, rmax] are painted until the porosity drops to porosity_target or below. Each sphere
+ * gets phase 1..n_phases uniformly (later spheres overwrite earlier ones). Deterministic in
+ * `seed` (splitmix64 stream). Returns the number of spheres; *porosity gets the final value. */
+int64_t rwnmr_synth_spheres(uint8_t *labels, int32_t nx, int32_t ny, int32_t nz, double rmin, double rmax,
+                            double porosity_target, int32_t n_phases, uint64_t seed, double *porosity);
+
+/* Host bit-block packer (BitBlock/bitBlock.cpp:138-221): solid = label != 0. Returns the block
+ * count; bdims = {blockColumns, blockRows, blockDepth}; blocks may be NULL to size the output. */
+int64_t rwnmr_pack_blocks(const uint8_t *labels, int32_t nx, int32_t ny, int32_t nz, uint64_t *blocks,
+                          int32_t *bdims);
+
+
+/* Walker placement statistics. */
+typedef struct rwnmr_placement_info
+{
+    uint32_t pores;    /* pore voxels considered */
+    double porosity;   /* image porosity */
+    double occupancy;  /* walkers / pores */
+    uint32_t clamped;  /* pore draws one past the end, clamped to the last pore */
+} rwnmr_placement_info;
+
+/* Creates n walkers the way NMR_Simulation::setWalkers does (NMR_Simulation.cpp:324-409,
+ * 1086-1454): RNG = std::mt19937 seeded with `seed` then discard(4096); one uint64 RNG seed per
+ * walker; positions by mode "random" (uniform over pore voxels), "point" (image centre) or
+ * "cubic" (centre +- deviation); then voxel division by 2^shift. Positions are in walk units.
+ * Returns 0, -1 on bad arguments, -2 if placement is impossible (no pores / point is solid). */
+int rwnmr_place_walkers(const uint64_t *blocks, int32_t nx, int32_t ny, int32_t nz, const char *mode,
+                        int32_t deviation, int32_t shift, uint64_t seed, int64_t n, int32_t *x0, int32_t *y0,
+                        int32_t *z0, uint64_t *seed0, rwnmr_placement_info *info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

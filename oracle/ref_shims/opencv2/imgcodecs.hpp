@@ -1,0 +1,2 @@
+// Forwards to the core shim; see core.hpp.
+#include "core.hpp"

@@ -1,0 +1,785 @@
+// C-ABI engine of the GB300 walker path: context, device memory, launches (include/rwnmr_gb300.h).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/rwnmr_gb300.h"
+#include "walk_kernels.cuh"
+
+using namespace rwnmr;
+
+namespace
+{
+typedef unsigned __int128 u128;
+
+template <typename T>
+struct DevBuf
+{
+    T *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n)
+    {
+        if (n <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc((void **)&p, std::max<size_t>(n, 1) * sizeof(T));
+        if (e == cudaSuccess) cap = std::max<size_t>(n, 1);
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+int phase_slots(int n_phases) { return n_phases <= 1 ? 1 : (n_phases == 2 ? 2 : 4); }
+int words_for(int n_phases) { return phase_slots(n_phases); }
+
+// table[n] = f^n as the FP64 repeated product (Walker/walker.cpp:229 applied n times) and its
+// fixed-point copy round(table[n] * 2^63).
+void build_tables(const double *f, int n_phases, int slots, int64_t nmax, std::vector<double> *t,
+                  std::vector<uint64_t> *fx)
+{
+    const size_t stride = (size_t)nmax + 1;
+    if (t) t->assign(slots * stride, 1.0);
+    if (fx) fx->assign(slots * stride, 1ull << 63);
+    for (int q = 0; q < n_phases; q++)
+    {
+        double v = 1.0;
+        for (int64_t k = 0; k <= nmax; k++)
+        {
+            if (t) (*t)[q * stride + k] = v;
+            if (fx) (*fx)[q * stride + k] = (uint64_t)std::nearbyint(std::ldexp(v, 63));
+            v = v * f[q];
+        }
+    }
+}
+
+double limbs_to_double(const unsigned long long *l)
+{
+    u128 v = (u128)l[0] + ((u128)l[1] << 21) + ((u128)l[2] << 42);
+    return std::ldexp((double)v, -63);
+}
+} // namespace
+
+struct rwnmr_ctx
+{
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t launches = 0;
+    double last_ms = 0.0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    bool has_image = false;
+    int nx = 0, ny = 0, nz = 0, bcols = 0, brows = 0, bdepth = 0, n_phases = 1, words = 1;
+    DevBuf<uint64_t> blocks;
+    DevBuf<uint8_t> labels;
+
+    int64_t n = 0;
+    bool has_walkers = false;
+    DevBuf<int32_t> x0, y0, z0, x, y, z;
+    DevBuf<uint64_t> seed0, seed;
+    DevBuf<uint32_t> coll;
+
+    DevBuf<uint64_t> tfx;
+    DevBuf<double> tfp;
+    DevBuf<unsigned long long> acc, hist;
+    DevBuf<unsigned> status;
+    DevBuf<double> grad, partial, partial_g, kbuf, Mbuf, gbuf;
+    DevBuf<int32_t> ibuf, disp;
+    DevBuf<double> energy;
+
+    rwnmr_status fail(rwnmr_status s, const char *fmt, ...)
+    {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        err = buf;
+        return s;
+    }
+    rwnmr_status cuda(cudaError_t e, const char *what)
+    {
+        if (e == cudaSuccess) return RWNMR_OK;
+        return fail(e == cudaErrorMemoryAllocation ? RWNMR_ERR_NOMEM : RWNMR_ERR_CUDA, "%s: %s", what,
+                    cudaGetErrorString(e));
+    }
+    DevImage image(int bc, int shift) const
+    {
+        DevImage im;
+        im.blocks = blocks.p;
+        im.nx = nx;
+        im.ny = ny;
+        im.nz = nz;
+        im.bcols = bcols;
+        im.bcr = bcols * brows;
+        im.bc = bc;
+        im.shift = shift;
+        return im;
+    }
+    WalkState state()
+    {
+        WalkState s;
+        s.n = n;
+        s.x0 = x0.p;
+        s.y0 = y0.p;
+        s.z0 = z0.p;
+        s.seed0 = seed0.p;
+        s.x = x.p;
+        s.y = y.p;
+        s.z = z.p;
+        s.seed = seed.p;
+        s.coll = coll.p;
+        return s;
+    }
+    rwnmr_status check_status(const char *what)
+    {
+        unsigned h = 0;
+        rwnmr_status r = cuda(cudaMemcpyAsync(&h, status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), what);
+        if (r != RWNMR_OK) return r;
+        r = cuda(cudaStreamSynchronize(stream), what);
+        if (r != RWNMR_OK) return r;
+        if (h & kStatusBadStart) return fail(RWNMR_ERR_INVALID, "%s: a walker starts outside the image", what);
+        if (h & kStatusBadLabel) return fail(RWNMR_ERR_INVALID, "%s: label exceeds the phase count", what);
+        if (h & kStatusHistRange) return fail(RWNMR_ERR_DEVICE, "%s: displacement histogram overflow", what);
+        return RWNMR_OK;
+    }
+};
+
+namespace
+{
+rwnmr_status need_run_state(rwnmr_ctx *ctx)
+{
+    if (!ctx) return RWNMR_ERR_INVALID;
+    if (!ctx->has_image) return ctx->fail(RWNMR_ERR_STATE, "no image uploaded");
+    if (!ctx->has_walkers) return ctx->fail(RWNMR_ERR_STATE, "no walkers uploaded");
+    return RWNMR_OK;
+}
+
+rwnmr_status check_geom(rwnmr_ctx *ctx, int bc, int shift)
+{
+    if (bc < RWNMR_BC_NOFLUX || bc > RWNMR_BC_MIRROR) return ctx->fail(RWNMR_ERR_INVALID, "unknown boundary condition %d", bc);
+    if (shift < 0 || shift > 10) return ctx->fail(RWNMR_ERR_INVALID, "voxel-division shift %d out of range 0..10", shift);
+    return RWNMR_OK;
+}
+
+rwnmr_status check_dfactor(rwnmr_ctx *ctx, const double *f)
+{
+    if (!f) return ctx->fail(RWNMR_ERR_INVALID, "dfactor is NULL");
+    for (int q = 0; q < ctx->n_phases; q++)
+        if (!(f[q] >= 0.0 && f[q] <= 1.0))
+            return ctx->fail(RWNMR_ERR_UNSUPPORTED, "decrease factor %g of phase %d outside [0, 1]", f[q], q);
+    return RWNMR_OK;
+}
+
+int bc_key(int bc, int shift) { return shift > 0 ? BC_GENERIC : bc; }
+
+dim3 walk_grid(int64_t n) { return dim3((unsigned)std::max<int64_t>(1, (n + kWalkThreads - 1) / kWalkThreads)); }
+} // namespace
+
+#define RW_TRY(expr)                                                                                                   \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        rwnmr_status _s = (expr);                                                                                      \
+        if (_s != RWNMR_OK) return _s;                                                                                 \
+    } while (0)
+#define RW_CUDA(ctx, expr, what) RW_TRY((ctx)->cuda((expr), (what)))
+
+extern "C" {
+
+const char *rwnmr_version(void) { return "rwnmr_gb300 0.1 (sm_103a)"; }
+
+rwnmr_status rwnmr_ctx_create(rwnmr_ctx **out, int device)
+{
+    if (!out) return RWNMR_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) return RWNMR_ERR_CUDA;
+    if (device < 0 || device >= count) return RWNMR_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return RWNMR_ERR_CUDA;
+    rwnmr_ctx *c = new rwnmr_ctx();
+    c->device = device;
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+        c->status.ensure(1) != cudaSuccess)
+    {
+        rwnmr_ctx_destroy(c);
+        return RWNMR_ERR_CUDA;
+    }
+    c->stream = c->own_stream;
+    *out = c;
+    return RWNMR_OK;
+}
+
+void rwnmr_ctx_destroy(rwnmr_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto *b : {&c->blocks}) b->release();
+    c->labels.release();
+    c->x0.release(); c->y0.release(); c->z0.release();
+    c->x.release(); c->y.release(); c->z.release();
+    c->seed0.release(); c->seed.release(); c->coll.release();
+    c->tfx.release(); c->tfp.release(); c->acc.release(); c->hist.release(); c->status.release();
+    c->grad.release(); c->partial.release(); c->partial_g.release(); c->kbuf.release(); c->Mbuf.release();
+    c->gbuf.release(); c->ibuf.release(); c->disp.release(); c->energy.release();
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+const char *rwnmr_last_error(const rwnmr_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+rwnmr_status rwnmr_ctx_set_stream(rwnmr_ctx *c, void *s)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    c->stream = s ? (cudaStream_t)s : c->own_stream;
+    return RWNMR_OK;
+}
+
+int64_t rwnmr_ctx_launch_count(const rwnmr_ctx *c) { return c ? c->launches : 0; }
+double rwnmr_ctx_last_kernel_ms(const rwnmr_ctx *c) { return c ? c->last_ms : 0.0; }
+
+// ---- image ------------------------------------------------------------------------------------
+static rwnmr_status set_dims(rwnmr_ctx *c, int32_t nx, int32_t ny, int32_t nz, int32_t n_phases)
+{
+    if (nx <= 0 || ny <= 0 || nz <= 0) return c->fail(RWNMR_ERR_INVALID, "image dims must be positive");
+    // The reference walks images with one slice on a separate 2D walker (Walker::walk_2D); this
+    // engine is the 3D walk, and its noflux reversal needs at least two voxels per axis.
+    if (nx < 2 || ny < 2 || nz < 2) return c->fail(RWNMR_ERR_UNSUPPORTED, "3D walks need at least 2 voxels per axis");
+    if ((int64_t)nx * ny * nz > (1ll << 40)) return c->fail(RWNMR_ERR_INVALID, "image too large");
+    if (n_phases < 1) return c->fail(RWNMR_ERR_INVALID, "n_phases must be >= 1");
+    if (n_phases > 4) return c->fail(RWNMR_ERR_UNSUPPORTED, "at most 4 solid phases are supported");
+    c->nx = nx;
+    c->ny = ny;
+    c->nz = nz;
+    c->bcols = (nx + 3) / 4;
+    c->brows = (ny + 3) / 4;
+    c->bdepth = (nz + 3) / 4;
+    c->n_phases = n_phases;
+    c->words = words_for(n_phases);
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_image_upload_labels(rwnmr_ctx *c, const uint8_t *labels, int32_t nx, int32_t ny, int32_t nz,
+                                       int32_t n_phases)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    if (!labels) return c->fail(RWNMR_ERR_INVALID, "labels is NULL");
+    c->has_image = false;
+    RW_TRY(set_dims(c, nx, ny, nz, n_phases));
+    cudaSetDevice(c->device);
+    const int64_t nb = (int64_t)c->bcols * c->brows * c->bdepth;
+    const size_t nvox = (size_t)nx * ny * nz;
+    RW_CUDA(c, c->labels.ensure(nvox), "image labels");
+    RW_CUDA(c, c->blocks.ensure((size_t)nb * c->words), "image blocks");
+    RW_CUDA(c, cudaMemcpyAsync(c->labels.p, labels, nvox, cudaMemcpyHostToDevice, c->stream), "labels upload");
+    RW_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(unsigned), c->stream), "status reset");
+    RW_CUDA(c, launch_pack_blocks(c->labels.p, nx, ny, nz, c->bcols, c->brows, nb, c->words, c->blocks.p, c->status.p,
+                                  c->stream), "pack kernel");
+    c->launches++;
+    RW_TRY(c->check_status("image packing"));
+    if (c->n_phases == 1) c->labels.release();
+    c->has_image = true;
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_image_upload(rwnmr_ctx *c, const uint64_t *blocks, int32_t nx, int32_t ny, int32_t nz,
+                                const uint8_t *labels, int32_t n_phases)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    if (!blocks) return c->fail(RWNMR_ERR_INVALID, "blocks is NULL");
+    if (labels)
+    {
+        RW_TRY(rwnmr_image_upload_labels(c, labels, nx, ny, nz, n_phases));
+        // the labels must describe the same solid voxels as the given bit-blocks
+        const int64_t nb = (int64_t)c->bcols * c->brows * c->bdepth;
+        std::vector<uint64_t> packed((size_t)nb * c->words);
+        RW_CUDA(c, cudaMemcpyAsync(packed.data(), c->blocks.p, packed.size() * 8, cudaMemcpyDeviceToHost, c->stream),
+                "blocks readback");
+        RW_CUDA(c, cudaStreamSynchronize(c->stream), "blocks readback");
+        for (int64_t b = 0; b < nb; b++)
+            if (packed[(size_t)b * c->words] != blocks[b])
+            {
+                c->has_image = false;
+                return c->fail(RWNMR_ERR_INVALID, "labels disagree with bit-block %lld", (long long)b);
+            }
+        return RWNMR_OK;
+    }
+    if (n_phases != 1) return c->fail(RWNMR_ERR_INVALID, "multi-phase images need labels");
+    c->has_image = false;
+    RW_TRY(set_dims(c, nx, ny, nz, 1));
+    cudaSetDevice(c->device);
+    const int64_t nb = (int64_t)c->bcols * c->brows * c->bdepth;
+    RW_CUDA(c, c->blocks.ensure((size_t)nb), "image blocks");
+    RW_CUDA(c, cudaMemcpyAsync(c->blocks.p, blocks, (size_t)nb * 8, cudaMemcpyHostToDevice, c->stream), "blocks upload");
+    RW_CUDA(c, cudaStreamSynchronize(c->stream), "blocks upload");
+    c->has_image = true;
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_image_download_blocks(rwnmr_ctx *c, uint64_t *out)
+{
+    if (!c || !out) return RWNMR_ERR_INVALID;
+    if (!c->has_image) return c->fail(RWNMR_ERR_STATE, "no image uploaded");
+    const int64_t nb = (int64_t)c->bcols * c->brows * c->bdepth;
+    if (c->words == 1)
+    {
+        RW_CUDA(c, cudaMemcpyAsync(out, c->blocks.p, (size_t)nb * 8, cudaMemcpyDeviceToHost, c->stream), "blocks download");
+    }
+    else
+    {
+        RW_CUDA(c, cudaMemcpy2DAsync(out, 8, c->blocks.p, (size_t)8 * c->words, 8, (size_t)nb, cudaMemcpyDeviceToHost,
+                                     c->stream), "blocks download");
+    }
+    RW_CUDA(c, cudaStreamSynchronize(c->stream), "blocks download");
+    return RWNMR_OK;
+}
+
+// ---- walkers ----------------------------------------------------------------------------------
+rwnmr_status rwnmr_walkers_upload(rwnmr_ctx *c, int64_t n, const int32_t *x0, const int32_t *y0, const int32_t *z0,
+                                  const uint64_t *seed0)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    if (n < 0 || n > (1ll << 31) - 1) return c->fail(RWNMR_ERR_INVALID, "walker count %lld out of range", (long long)n);
+    if (n > 0 && (!x0 || !y0 || !z0 || !seed0)) return c->fail(RWNMR_ERR_INVALID, "walker arrays must not be NULL");
+    c->has_walkers = false;
+    cudaSetDevice(c->device);
+    const size_t m = (size_t)std::max<int64_t>(n, 1);
+    RW_CUDA(c, c->x0.ensure(m), "walkers"); RW_CUDA(c, c->y0.ensure(m), "walkers"); RW_CUDA(c, c->z0.ensure(m), "walkers");
+    RW_CUDA(c, c->x.ensure(m), "walkers"); RW_CUDA(c, c->y.ensure(m), "walkers"); RW_CUDA(c, c->z.ensure(m), "walkers");
+    RW_CUDA(c, c->seed0.ensure(m), "walkers"); RW_CUDA(c, c->seed.ensure(m), "walkers");
+    RW_CUDA(c, c->coll.ensure(m * 4), "walkers");
+    if (n > 0)
+    {
+        const size_t b4 = (size_t)n * 4, b8 = (size_t)n * 8;
+        RW_CUDA(c, cudaMemcpyAsync(c->x0.p, x0, b4, cudaMemcpyHostToDevice, c->stream), "walkers upload");
+        RW_CUDA(c, cudaMemcpyAsync(c->y0.p, y0, b4, cudaMemcpyHostToDevice, c->stream), "walkers upload");
+        RW_CUDA(c, cudaMemcpyAsync(c->z0.p, z0, b4, cudaMemcpyHostToDevice, c->stream), "walkers upload");
+        RW_CUDA(c, cudaMemcpyAsync(c->seed0.p, seed0, b8, cudaMemcpyHostToDevice, c->stream), "walkers upload");
+        RW_CUDA(c, cudaMemcpyAsync(c->x.p, c->x0.p, b4, cudaMemcpyDeviceToDevice, c->stream), "walkers init");
+        RW_CUDA(c, cudaMemcpyAsync(c->y.p, c->y0.p, b4, cudaMemcpyDeviceToDevice, c->stream), "walkers init");
+        RW_CUDA(c, cudaMemcpyAsync(c->z.p, c->z0.p, b4, cudaMemcpyDeviceToDevice, c->stream), "walkers init");
+        RW_CUDA(c, cudaMemcpyAsync(c->seed.p, c->seed0.p, b8, cudaMemcpyDeviceToDevice, c->stream), "walkers init");
+        RW_CUDA(c, cudaMemsetAsync(c->coll.p, 0, b4 * 4, c->stream), "walkers init");
+    }
+    RW_CUDA(c, cudaStreamSynchronize(c->stream), "walkers upload");
+    c->n = n;
+    c->has_walkers = true;
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_walkers_download(rwnmr_ctx *c, int32_t *x, int32_t *y, int32_t *z, uint64_t *seed, uint32_t *coll)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    if (!c->has_walkers) return c->fail(RWNMR_ERR_STATE, "no walkers uploaded");
+    const int64_t n = c->n;
+    if (n == 0) return RWNMR_OK;
+    const size_t b4 = (size_t)n * 4;
+    if (x) RW_CUDA(c, cudaMemcpyAsync(x, c->x.p, b4, cudaMemcpyDeviceToHost, c->stream), "walkers download");
+    if (y) RW_CUDA(c, cudaMemcpyAsync(y, c->y.p, b4, cudaMemcpyDeviceToHost, c->stream), "walkers download");
+    if (z) RW_CUDA(c, cudaMemcpyAsync(z, c->z.p, b4, cudaMemcpyDeviceToHost, c->stream), "walkers download");
+    if (seed) RW_CUDA(c, cudaMemcpyAsync(seed, c->seed.p, b4 * 2, cudaMemcpyDeviceToHost, c->stream), "walkers download");
+    std::vector<uint32_t> tmp;
+    const int P = c->n_phases;
+    if (coll)
+    {
+        tmp.resize((size_t)n * P);
+        RW_CUDA(c, cudaMemcpyAsync(tmp.data(), c->coll.p, b4 * P, cudaMemcpyDeviceToHost, c->stream), "walkers download");
+    }
+    RW_CUDA(c, cudaStreamSynchronize(c->stream), "walkers download");
+    if (coll)
+        for (int64_t i = 0; i < n; i++)
+            for (int q = 0; q < P; q++) coll[(size_t)i * P + q] = tmp[(size_t)q * n + i];
+    return RWNMR_OK;
+}
+
+// ---- CPMG -------------------------------------------------------------------------------------
+rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *echo_sum, uint64_t *echo_fx,
+                            uint64_t *echo_coll)
+{
+    RW_TRY(need_run_state(c));
+    if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
+    RW_TRY(check_geom(c, p->bc, p->shift));
+    RW_TRY(check_dfactor(c, p->dfactor));
+    if (p->n_echoes < 0 || p->steps_per_echo < 1) return c->fail(RWNMR_ERR_INVALID, "bad echo count / steps per echo");
+    const int64_t nmax = (int64_t)p->n_echoes * p->steps_per_echo;
+    if (nmax > (1ll << 28)) return c->fail(RWNMR_ERR_UNSUPPORTED, "walk of %lld steps too long", (long long)nmax);
+    cudaSetDevice(c->device);
+    const int slots = phase_slots(c->n_phases);
+    const int K = 3 + slots;
+    std::vector<uint64_t> fx;
+    build_tables(p->dfactor, c->n_phases, slots, nmax, nullptr, &fx);
+    RW_CUDA(c, c->tfx.ensure(fx.size()), "tables");
+    RW_CUDA(c, c->acc.ensure((size_t)(p->n_echoes + 1) * K), "echo accumulators");
+    RW_CUDA(c, cudaMemcpyAsync(c->tfx.p, fx.data(), fx.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables upload");
+    RW_CUDA(c, cudaMemsetAsync(c->acc.p, 0, (size_t)(p->n_echoes + 1) * K * 8, c->stream), "accumulator reset");
+    RW_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(unsigned), c->stream), "status reset");
+
+    int chunk = p->echoes_per_launch > 0 ? p->echoes_per_launch : std::max(32, (4096 / p->steps_per_echo) / 32 * 32);
+    const DevImage im = c->image(p->bc, p->shift);
+    const WalkState st = c->state();
+    CpmgLaunch L{};
+    L.steps_per_echo = p->steps_per_echo;
+    L.record = 1;
+    L.tfx = c->tfx.p;
+    L.tstride = (int)(nmax + 1);
+    L.acc = c->acc.p;
+    L.status = c->status.p;
+    RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
+    if (c->n > 0)
+    {
+        if (p->n_echoes == 0)
+        {
+            L.e_begin = 0;
+            L.e_end = 0;
+            L.from_initial = 1;
+            RW_CUDA(c, launch_cpmg_walk(bc_key(p->bc, p->shift), slots, im, st, L, walk_grid(c->n), c->stream), "cpmg kernel");
+            c->launches++;
+        }
+        for (int e = 0; e < p->n_echoes; e += chunk)
+        {
+            L.e_begin = e;
+            L.e_end = std::min(p->n_echoes, e + chunk);
+            L.from_initial = e == 0;
+            RW_CUDA(c, launch_cpmg_walk(bc_key(p->bc, p->shift), slots, im, st, L, walk_grid(c->n), c->stream), "cpmg kernel");
+            c->launches++;
+        }
+    }
+    RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
+    std::vector<unsigned long long> acc((size_t)(p->n_echoes + 1) * K);
+    RW_CUDA(c, cudaMemcpyAsync(acc.data(), c->acc.p, acc.size() * 8, cudaMemcpyDeviceToHost, c->stream), "echo readback");
+    RW_TRY(c->check_status("cpmg walk"));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->last_ms = ms;
+    for (int e = 0; e <= p->n_echoes; e++)
+    {
+        const unsigned long long *a = &acc[(size_t)e * K];
+        if (echo_sum) echo_sum[e] = limbs_to_double(a);
+        if (echo_fx)
+            for (int k = 0; k < 3; k++) echo_fx[(size_t)e * 3 + k] = a[k];
+        if (echo_coll && e > 0)
+            for (int q = 0; q < c->n_phases; q++) echo_coll[(size_t)(e - 1) * c->n_phases + q] = a[3 + q];
+    }
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const double *grad_echo, double *grad_dfactor)
+{
+    RW_TRY(need_run_state(c));
+    if (!p || !grad_echo || !grad_dfactor) return c->fail(RWNMR_ERR_INVALID, "NULL argument");
+    RW_TRY(check_geom(c, p->bc, p->shift));
+    RW_TRY(check_dfactor(c, p->dfactor));
+    if (p->n_echoes < 0 || p->steps_per_echo < 1) return c->fail(RWNMR_ERR_INVALID, "bad echo count / steps per echo");
+    const int64_t nmax = (int64_t)p->n_echoes * p->steps_per_echo;
+    if (nmax > (1ll << 28)) return c->fail(RWNMR_ERR_UNSUPPORTED, "walk too long");
+    cudaSetDevice(c->device);
+    const int slots = phase_slots(c->n_phases);
+    // derivative tables: dt[q][k] = k * f_q^(k-1) (so d/df_q of walker energy is dt[q][c_q] * prod_{r != q} t[r][c_r])
+    std::vector<double> t;
+    build_tables(p->dfactor, c->n_phases, slots, nmax, &t, nullptr);
+    const size_t stride = (size_t)nmax + 1;
+    std::vector<double> tab(2 * slots * stride);
+    for (int q = 0; q < slots; q++)
+        for (size_t k = 0; k < stride; k++)
+        {
+            tab[q * stride + k] = t[q * stride + k];
+            tab[(slots + q) * stride + k] = k == 0 ? 0.0 : (double)k * t[q * stride + k - 1];
+        }
+    const dim3 grid = walk_grid(c->n);
+    RW_CUDA(c, c->tfp.ensure(tab.size()), "tables");
+    RW_CUDA(c, c->grad.ensure((size_t)p->n_echoes + 1), "grad");
+    RW_CUDA(c, c->partial.ensure((size_t)grid.x * slots), "partials");
+    RW_CUDA(c, cudaMemcpyAsync(c->tfp.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables upload");
+    RW_CUDA(c, cudaMemcpyAsync(c->grad.p, grad_echo, ((size_t)p->n_echoes + 1) * 8, cudaMemcpyHostToDevice, c->stream),
+            "grad upload");
+    RW_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(unsigned), c->stream), "status reset");
+    AdjointLaunch L{};
+    L.n_echoes = p->n_echoes;
+    L.steps_per_echo = p->steps_per_echo;
+    L.t = c->tfp.p;
+    L.tstride = (int)stride;
+    L.grad = c->grad.p;
+    L.partial = c->partial.p;
+    L.status = c->status.p;
+    RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
+    if (c->n > 0)
+    {
+        RW_CUDA(c, launch_cpmg_adjoint(bc_key(p->bc, p->shift), slots, c->image(p->bc, p->shift), c->state(), L, grid,
+                                       c->stream), "adjoint kernel");
+        c->launches++;
+    }
+    RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
+    std::vector<double> part((size_t)grid.x * slots, 0.0);
+    if (c->n > 0)
+        RW_CUDA(c, cudaMemcpyAsync(part.data(), c->partial.p, part.size() * 8, cudaMemcpyDeviceToHost, c->stream),
+                "partials readback");
+    RW_TRY(c->check_status("cpmg adjoint"));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->last_ms = ms;
+    for (int q = 0; q < c->n_phases; q++)
+    {
+        double s = 0.0;
+        for (unsigned b = 0; b < grid.x; b++) s += part[(size_t)b * slots + q];
+        grad_dfactor[q] = s;
+    }
+    // echo 0 does not depend on the decrease factors
+    return RWNMR_OK;
+}
+
+// ---- collision mapping ------------------------------------------------------------------------
+rwnmr_status rwnmr_map_run(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions)
+{
+    RW_TRY(need_run_state(c));
+    RW_TRY(check_geom(c, bc, shift));
+    if (steps < 0 || steps > (1ll << 31) - 1) return c->fail(RWNMR_ERR_INVALID, "bad step count");
+    cudaSetDevice(c->device);
+    const int slots = phase_slots(c->n_phases);
+    RW_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(unsigned), c->stream), "status reset");
+    CpmgLaunch L{};
+    L.record = 0;
+    L.status = c->status.p;
+    L.tstride = 1;
+    const DevImage im = c->image(bc, shift);
+    const WalkState st = c->state();
+    const int64_t chunk = 1 << 14;
+    RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
+    if (c->n > 0)
+    {
+        if (steps == 0)
+        {
+            L.e_begin = 0;
+            L.e_end = 0;
+            L.from_initial = 1;
+            L.steps_per_echo = 1;
+            RW_CUDA(c, launch_cpmg_walk(bc_key(bc, shift), slots, im, st, L, walk_grid(c->n), c->stream), "map kernel");
+            c->launches++;
+        }
+        for (int64_t s = 0; s < steps; s += chunk)
+        {
+            L.e_begin = 0;
+            L.e_end = 1;
+            L.steps_per_echo = (int)std::min<int64_t>(chunk, steps - s);
+            L.from_initial = s == 0;
+            RW_CUDA(c, launch_cpmg_walk(bc_key(bc, shift), slots, im, st, L, walk_grid(c->n), c->stream), "map kernel");
+            c->launches++;
+        }
+    }
+    RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
+    RW_TRY(c->check_status("map walk"));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->last_ms = ms;
+    if (collisions && c->n > 0)
+    {
+        const int P = c->n_phases;
+        std::vector<uint32_t> tmp((size_t)c->n * P);
+        RW_CUDA(c, cudaMemcpyAsync(tmp.data(), c->coll.p, tmp.size() * 4, cudaMemcpyDeviceToHost, c->stream), "readback");
+        RW_CUDA(c, cudaStreamSynchronize(c->stream), "readback");
+        for (int64_t i = 0; i < c->n; i++)
+        {
+            uint32_t s = 0;
+            for (int q = 0; q < P; q++) s += tmp[(size_t)q * c->n + i];
+            collisions[i] = s;
+        }
+    }
+    return RWNMR_OK;
+}
+
+// ---- PFGSE ------------------------------------------------------------------------------------
+static rwnmr_status pfgse_impl(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double *M, double *esum, uint64_t *msd,
+                               bool want_grad, double kscale, const double *dir, double *dMdg)
+{
+    RW_TRY(need_run_state(c));
+    if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
+    RW_TRY(check_geom(c, p->bc, p->shift));
+    RW_TRY(check_dfactor(c, p->dfactor));
+    if (p->n_delta < 0 || p->n_g < 0 || (p->n_delta > 0 && !p->steps) || (p->n_g > 0 && !p->kvec))
+        return c->fail(RWNMR_ERR_INVALID, "bad PFGSE sizes");
+    for (int i = 0; i < p->n_delta; i++)
+        if (p->steps[i] < 0 || (i && p->steps[i] < p->steps[i - 1]))
+            return c->fail(RWNMR_ERR_INVALID, "PFGSE steps must be non-negative and non-decreasing");
+    const int smax = p->n_delta ? p->steps[p->n_delta - 1] : 0;
+    if (smax > (1 << 20)) return c->fail(RWNMR_ERR_UNSUPPORTED, "PFGSE walks are limited to 2^20 steps");
+    cudaSetDevice(c->device);
+    // gradient along a single axis -> displacement histogram path
+    int axis = -1;
+    {
+        bool nz[3] = {false, false, false};
+        for (int j = 0; j < p->n_g; j++)
+            for (int a = 0; a < 3; a++) nz[a] |= p->kvec[3 * j + a] != 0.0;
+        int cnt = nz[0] + nz[1] + nz[2];
+        if (cnt == 0) axis = 2;
+        else if (cnt == 1) axis = nz[0] ? 0 : (nz[1] ? 1 : 2);
+        if (want_grad && dir)
+        {
+            int dn = (dir[0] != 0.0) + (dir[1] != 0.0) + (dir[2] != 0.0);
+            if (dn != 1 || (axis >= 0 && dir[axis] == 0.0 && cnt)) axis = -1;
+            else if (cnt == 0) axis = dir[0] != 0.0 ? 0 : (dir[1] != 0.0 ? 1 : 2);
+        }
+        if (p->n_g > kDirectMaxG && axis < 0)
+            return c->fail(RWNMR_ERR_UNSUPPORTED, "general-direction PFGSE handles at most %d gradient points", kDirectMaxG);
+    }
+    const int slots = phase_slots(c->n_phases);
+    std::vector<uint64_t> fx;
+    std::vector<double> t;
+    build_tables(p->dfactor, c->n_phases, slots, smax, axis < 0 ? &t : nullptr, &fx);
+    const int nd = p->n_delta, ng = p->n_g;
+    const int hh = smax;
+    const size_t nbins = 2 * (size_t)hh + 1;
+    RW_CUDA(c, c->tfx.ensure(fx.size()), "tables");
+    RW_CUDA(c, cudaMemcpyAsync(c->tfx.p, fx.data(), fx.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables");
+    if (axis < 0)
+    {
+        RW_CUDA(c, c->tfp.ensure(t.size()), "tables");
+        RW_CUDA(c, cudaMemcpyAsync(c->tfp.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables");
+        RW_CUDA(c, c->disp.ensure((size_t)std::max(nd, 1) * std::max<int64_t>(c->n, 1) * 3), "displacements");
+        RW_CUDA(c, c->energy.ensure((size_t)std::max(nd, 1) * std::max<int64_t>(c->n, 1)), "energies");
+    }
+    else
+    {
+        RW_CUDA(c, c->hist.ensure((size_t)std::max(nd, 1) * nbins * 2), "histograms");
+        RW_CUDA(c, cudaMemsetAsync(c->hist.p, 0, (size_t)nd * nbins * 16, c->stream), "histogram reset");
+    }
+    RW_CUDA(c, c->acc.ensure((size_t)std::max(nd, 1) * 6), "accumulators");
+    RW_CUDA(c, cudaMemsetAsync(c->acc.p, 0, (size_t)nd * 6 * 8, c->stream), "accumulator reset");
+    RW_CUDA(c, c->ibuf.ensure((size_t)std::max(nd, 1)), "steps");
+    if (nd) RW_CUDA(c, cudaMemcpyAsync(c->ibuf.p, p->steps, (size_t)nd * 4, cudaMemcpyHostToDevice, c->stream), "steps");
+    RW_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(unsigned), c->stream), "status reset");
+
+    PfgseLaunch L{};
+    L.n_delta = nd;
+    L.steps = c->ibuf.p;
+    L.tfx = c->tfx.p;
+    L.t = c->tfp.p;
+    L.tstride = smax + 1;
+    L.acc = c->acc.p;
+    L.axis = axis;
+    L.hist_half = hh;
+    L.hist = c->hist.p;
+    L.disp = c->disp.p;
+    L.energy = c->energy.p;
+    L.status = c->status.p;
+    RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
+    if (c->n > 0 && nd > 0)
+    {
+        RW_CUDA(c, launch_pfgse_walk(bc_key(p->bc, p->shift), slots, c->image(p->bc, p->shift), c->state(), L,
+                                     walk_grid(c->n), c->stream), "pfgse kernel");
+        c->launches++;
+    }
+    RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
+    // phase sums
+    std::vector<double> Mh((size_t)nd * ng, 0.0), Gh((size_t)nd * ng, 0.0);
+    if (nd > 0 && ng > 0)
+    {
+        RW_CUDA(c, c->Mbuf.ensure((size_t)nd * ng), "phase buffer");
+        RW_CUDA(c, c->gbuf.ensure((size_t)nd * ng), "phase buffer");
+        if (axis >= 0)
+        {
+            std::vector<double> ka(ng);
+            for (int j = 0; j < ng; j++) ka[j] = p->kvec[3 * j + axis];
+            RW_CUDA(c, c->kbuf.ensure((size_t)ng * 3), "k buffer");
+            RW_CUDA(c, cudaMemcpyAsync(c->kbuf.p, ka.data(), (size_t)ng * 8, cudaMemcpyHostToDevice, c->stream), "k upload");
+            PhaseLaunch PL{};
+            PL.hist = c->hist.p;
+            PL.hist_half = hh;
+            PL.kaxis = c->kbuf.p;
+            PL.res = p->res;
+            PL.kscale_axis = want_grad ? kscale * (dir ? dir[axis] : 0.0) : 0.0;
+            PL.M = c->Mbuf.p;
+            PL.dMdg = want_grad ? c->gbuf.p : nullptr;
+            RW_CUDA(c, launch_pfgse_phase(PL, nd, ng, c->stream), "phase kernel");
+            c->launches++;
+            RW_CUDA(c, cudaMemcpyAsync(Mh.data(), c->Mbuf.p, Mh.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
+            if (want_grad)
+                RW_CUDA(c, cudaMemcpyAsync(Gh.data(), c->gbuf.p, Gh.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
+        }
+        else if (c->n > 0)
+        {
+            const int blocks = (int)std::min<int64_t>(1184, (c->n + 255) / 256);
+            RW_CUDA(c, c->kbuf.ensure((size_t)ng * 3), "k buffer");
+            RW_CUDA(c, cudaMemcpyAsync(c->kbuf.p, p->kvec, (size_t)ng * 24, cudaMemcpyHostToDevice, c->stream), "k upload");
+            RW_CUDA(c, c->partial.ensure((size_t)nd * ng * blocks), "partials");
+            RW_CUDA(c, c->partial_g.ensure((size_t)nd * ng * blocks), "partials");
+            DirectLaunch DL{};
+            DL.n = c->n;
+            DL.n_g = ng;
+            DL.disp = c->disp.p;
+            DL.energy = c->energy.p;
+            DL.kvec = c->kbuf.p;
+            DL.res = p->res;
+            DL.grad_on = want_grad ? 1 : 0;
+            DL.kscale = kscale;
+            for (int a = 0; a < 3; a++) DL.dir[a] = dir ? dir[a] : 0.0;
+            DL.partial = c->partial.p;
+            DL.partial_g = c->partial_g.p;
+            RW_CUDA(c, launch_pfgse_direct(DL, nd, blocks, c->stream), "direct phase kernel");
+            c->launches++;
+            std::vector<double> part((size_t)nd * ng * blocks), partg;
+            RW_CUDA(c, cudaMemcpyAsync(part.data(), c->partial.p, part.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
+            if (want_grad)
+            {
+                partg.resize(part.size());
+                RW_CUDA(c, cudaMemcpyAsync(partg.data(), c->partial_g.p, partg.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
+            }
+            RW_CUDA(c, cudaStreamSynchronize(c->stream), "readback");
+            for (size_t k = 0; k < (size_t)nd * ng; k++)
+            {
+                double s = 0.0, g = 0.0;
+                for (int b = 0; b < blocks; b++)
+                {
+                    s += part[k * blocks + b];
+                    if (want_grad) g += partg[k * blocks + b];
+                }
+                Mh[k] = s;
+                Gh[k] = g;
+            }
+        }
+    }
+    std::vector<unsigned long long> acc((size_t)nd * 6);
+    if (nd) RW_CUDA(c, cudaMemcpyAsync(acc.data(), c->acc.p, acc.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
+    RW_TRY(c->check_status("pfgse walk"));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->last_ms = ms;
+    if (M) std::copy(Mh.begin(), Mh.end(), M);
+    if (dMdg) std::copy(Gh.begin(), Gh.end(), dMdg);
+    for (int i = 0; i < nd; i++)
+    {
+        if (esum) esum[i] = limbs_to_double(&acc[(size_t)i * 6]);
+        if (msd)
+            for (int a = 0; a < 3; a++) msd[(size_t)i * 3 + a] = acc[(size_t)i * 6 + 3 + a];
+    }
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_pfgse_run(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double *M, double *esum, uint64_t *msd)
+{
+    return pfgse_impl(c, p, M, esum, msd, false, 0.0, nullptr, nullptr);
+}
+
+rwnmr_status rwnmr_pfgse_grad_g(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double kscale, const double *dir,
+                                double *dMdg)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    if (!dir || !dMdg) return c->fail(RWNMR_ERR_INVALID, "NULL argument");
+    return pfgse_impl(c, p, nullptr, nullptr, nullptr, true, kscale, dir, dMdg);
+}
+
+} // extern "C"

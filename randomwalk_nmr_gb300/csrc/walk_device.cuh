@@ -1,0 +1,286 @@
+// Device-side walker step for the GB300 walker engine.
+//
+// One walker step is the reference's Walker::walk_3D / map_3D (Walker/walker.cpp:197-231) and the
+// CUDA CPMG_walk_* / map_3D_* / PFG_map_* kernels (NMR_cpmg_cuda.cpp:37-139, 300-402, 574-676):
+//   xorshift64 -> direction (state mod 6) -> [noflux: reverse a move off the image] -> next
+//   position -> image-space lookup -> bit test in the 4x4x4 bit-block -> move, or count a
+//   collision on the solid voxel's phase.
+// The formulation here is branch-free integer code:
+//   * mod 6 of the 64-bit state uses 2^32 = 1 (mod 3): a mod 3 = (hi + lo + carry) mod 3, and the
+//     parity of a picks r or r+3. This equals the reference's digit-sum mod6 (walker.h:566-582)
+//     for every 64-bit value.
+//   * periodic and mirror boundaries keep the image-space coordinate incrementally (wrap, or
+//     stay-and-flip the tile orientation) instead of the per-step modulo of
+//     NMR_cpmg_cuda.cpp:1991-2015; positions stay unwrapped like the reference's.
+//   * voxel division (shift > 0) takes the general path that applies the reference's formulas.
+#pragma once
+#include <cstdint>
+
+namespace rwnmr
+{
+
+enum
+{
+    BC_NOFLUX = 0,
+    BC_PERIODIC = 1,
+    BC_MIRROR = 2,
+    BC_GENERIC = 3 // any bc with voxel division: runtime bc, reference formulas
+};
+
+// Bit-block image on the device. Each block holds W consecutive 64-bit words: word 0 is the solid
+// mask, words 1..W-1 are bit-planes of the solid voxel's phase index (multi-phase images only).
+struct DevImage
+{
+    const uint64_t *__restrict__ blocks;
+    int32_t nx, ny, nz;
+    int32_t bcols;
+    int32_t bcr; // bcols * brows
+    int32_t bc;  // runtime boundary condition (BC_GENERIC path)
+    int32_t shift;
+};
+
+__device__ __forceinline__ uint64_t xorshift64(uint64_t x)
+{
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    return x;
+}
+
+// state mod 6, see the file comment.
+__device__ __forceinline__ uint32_t mod6(uint64_t a)
+{
+    uint32_t lo = (uint32_t)a, hi = (uint32_t)(a >> 32);
+    uint32_t t = lo + hi;
+    t += (t < lo) ? 1u : 0u; // carry of lo + hi is worth 2^32 = 1 (mod 3)
+    uint32_t r3 = t % 3u;
+    return r3 + 3u * ((r3 ^ lo) & 1u);
+}
+
+// Reference periodic / mirror image index for the generic path (NMR_cpmg_cuda.cpp:1991-2015).
+__device__ __forceinline__ int map_periodic(int local, int shift, int dim)
+{
+    int g = (local >> shift) % dim;
+    return g < 0 ? g + dim : g;
+}
+__device__ __forceinline__ int map_mirror(int local, int shift, int dim)
+{
+    int g = local >> shift;
+    int img = g % dim;
+    if (img < 0) img += dim;
+    int mirror = (g > 0) ? (g / dim) % 2 : ((-g - 1 + dim) / dim) % 2;
+    return mirror ? (dim - 1 - img) : img;
+}
+// Tile orientation (+1 / -1) of a mirrored coordinate, used to seed the incremental mirror path.
+__device__ __forceinline__ int mirror_orientation(int g, int dim)
+{
+    int mirror = (g > 0) ? (g / dim) % 2 : ((-g - 1 + dim) / dim) % 2;
+    return mirror ? -1 : 1;
+}
+
+// Walker position: real (unwrapped) walk-grid coordinates plus, for periodic/mirror without
+// voxel division, the image coordinates and mirror orientations carried incrementally.
+struct WalkerPos
+{
+    int x, y, z;
+    int ix, iy, iz;
+    int ox, oy, oz;
+};
+
+template <int BC>
+__device__ __forceinline__ void init_image_coords(const DevImage &im, WalkerPos &p)
+{
+    if (BC == BC_PERIODIC)
+    {
+        p.ix = map_periodic(p.x, 0, im.nx);
+        p.iy = map_periodic(p.y, 0, im.ny);
+        p.iz = map_periodic(p.z, 0, im.nz);
+    }
+    else if (BC == BC_MIRROR)
+    {
+        p.ix = map_mirror(p.x, 0, im.nx);
+        p.iy = map_mirror(p.y, 0, im.ny);
+        p.iz = map_mirror(p.z, 0, im.nz);
+        p.ox = mirror_orientation(p.x, im.nx);
+        p.oy = mirror_orientation(p.y, im.ny);
+        p.oz = mirror_orientation(p.z, im.nz);
+    }
+    else
+    {
+        p.ix = p.x;
+        p.iy = p.y;
+        p.iz = p.z;
+    }
+}
+
+// Returns true if a walker may start at p: inside the image for noflux (in walk units).
+template <int BC>
+__device__ __forceinline__ bool start_ok(const DevImage &im, const WalkerPos &p)
+{
+    if (BC == BC_NOFLUX || (BC == BC_GENERIC && im.bc == BC_NOFLUX))
+    {
+        int s = (BC == BC_GENERIC) ? im.shift : 0;
+        return (unsigned)(p.x >> s) < (unsigned)im.nx && (unsigned)(p.y >> s) < (unsigned)im.ny &&
+               (unsigned)(p.z >> s) < (unsigned)im.nz && p.x >= 0 && p.y >= 0 && p.z >= 0;
+    }
+    return true;
+}
+
+// One step. On return `wall` tells whether the move was rejected; if so `phase` is the solid
+// voxel's phase index (0 for single-phase images). W = words per block.
+template <int BC, int W>
+__device__ __forceinline__ void walker_step(const DevImage &im, WalkerPos &p, uint64_t &seed, bool &wall, int &phase)
+{
+    seed = xorshift64(seed);
+    const uint32_t r = mod6(seed); // 0:N(-y) 1:W(-x) 2:S(+y) 3:E(+x) 4:Up(+z) 5:Down(-z)
+    int dx = (r == 3u) - (r == 1u);
+    int dy = (r == 2u) - (r == 0u);
+    int dz = (r == 4u) - (r == 5u);
+
+    int tx, ty, tz;    // candidate real position
+    int cix, ciy, ciz; // candidate image position
+    int cox = 0, coy = 0, coz = 0;
+    if (BC == BC_NOFLUX)
+    {
+        // A move off the image is reversed (walker.h:444-491): the walker steps inward.
+        if ((unsigned)(p.x + dx) >= (unsigned)im.nx) dx = -dx;
+        if ((unsigned)(p.y + dy) >= (unsigned)im.ny) dy = -dy;
+        if ((unsigned)(p.z + dz) >= (unsigned)im.nz) dz = -dz;
+        tx = p.x + dx;
+        ty = p.y + dy;
+        tz = p.z + dz;
+        cix = tx;
+        ciy = ty;
+        ciz = tz;
+    }
+    else if (BC == BC_PERIODIC)
+    {
+        tx = p.x + dx;
+        ty = p.y + dy;
+        tz = p.z + dz;
+        cix = p.ix + dx;
+        ciy = p.iy + dy;
+        ciz = p.iz + dz;
+        cix = cix < 0 ? im.nx - 1 : (cix >= im.nx ? 0 : cix);
+        ciy = ciy < 0 ? im.ny - 1 : (ciy >= im.ny ? 0 : ciy);
+        ciz = ciz < 0 ? im.nz - 1 : (ciz >= im.nz ? 0 : ciz);
+    }
+    else if (BC == BC_MIRROR)
+    {
+        tx = p.x + dx;
+        ty = p.y + dy;
+        tz = p.z + dz;
+        // Crossing a tile edge keeps the image index and flips the tile orientation.
+        cix = p.ix + p.ox * dx;
+        ciy = p.iy + p.oy * dy;
+        ciz = p.iz + p.oz * dz;
+        cox = p.ox;
+        coy = p.oy;
+        coz = p.oz;
+        if ((unsigned)cix >= (unsigned)im.nx) { cix = p.ix; cox = -p.ox; }
+        if ((unsigned)ciy >= (unsigned)im.ny) { ciy = p.iy; coy = -p.oy; }
+        if ((unsigned)ciz >= (unsigned)im.nz) { ciz = p.iz; coz = -p.oz; }
+    }
+    else // BC_GENERIC: voxel division, reference formulas (NMR_cpmg_cuda.cpp:1847-2015)
+    {
+        const int s = im.shift;
+        if (im.bc == BC_NOFLUX)
+        {
+            if ((unsigned)((p.x >> s) + dx) >= (unsigned)im.nx) dx = -dx;
+            if ((unsigned)((p.y >> s) + dy) >= (unsigned)im.ny) dy = -dy;
+            if ((unsigned)((p.z >> s) + dz) >= (unsigned)im.nz) dz = -dz;
+        }
+        tx = p.x + dx;
+        ty = p.y + dy;
+        tz = p.z + dz;
+        if (im.bc == BC_PERIODIC)
+        {
+            cix = map_periodic(tx, s, im.nx);
+            ciy = map_periodic(ty, s, im.ny);
+            ciz = map_periodic(tz, s, im.nz);
+        }
+        else if (im.bc == BC_MIRROR)
+        {
+            cix = map_mirror(tx, s, im.nx);
+            ciy = map_mirror(ty, s, im.ny);
+            ciz = map_mirror(tz, s, im.nz);
+        }
+        else
+        {
+            cix = tx >> s;
+            ciy = ty >> s;
+            ciz = tz >> s;
+        }
+    }
+
+    const int64_t blk = (int64_t)(cix >> 2) + (int64_t)(ciy >> 2) * im.bcols + (int64_t)(ciz >> 2) * im.bcr;
+    const uint32_t bit = (uint32_t)((cix & 3) | ((ciy & 3) << 2) | ((ciz & 3) << 4));
+    const uint64_t *bp = im.blocks + blk * W;
+    uint64_t solid;
+    phase = 0;
+    if (W == 1)
+    {
+        solid = __ldg(bp);
+    }
+    else if (W == 2)
+    {
+        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(bp));
+        solid = v.x;
+        phase = (int)((v.y >> bit) & 1ull);
+    }
+    else
+    {
+        ulonglong2 v0 = __ldg(reinterpret_cast<const ulonglong2 *>(bp));
+        ulonglong2 v1 = __ldg(reinterpret_cast<const ulonglong2 *>(bp) + 1);
+        solid = v0.x;
+        phase = (int)(((v0.y >> bit) & 1ull) | (((v1.x >> bit) & 1ull) << 1) | (((v1.y >> bit) & 1ull) << 2));
+    }
+    wall = ((solid >> bit) & 1ull) != 0;
+    if (!wall)
+    {
+        p.x = tx;
+        p.y = ty;
+        p.z = tz;
+        if (BC == BC_PERIODIC || BC == BC_MIRROR)
+        {
+            p.ix = cix;
+            p.iy = ciy;
+            p.iz = ciz;
+        }
+        if (BC == BC_MIRROR)
+        {
+            p.ox = cox;
+            p.oy = coy;
+            p.oz = coz;
+        }
+    }
+}
+
+// Fixed-point energy (scale 2^63) of a walker with per-phase collision counts c[]: the product of
+// the per-phase tables, each table[n] = round(f^n * 2^63) with f^n the FP64 repeated product.
+__device__ __forceinline__ uint64_t fx_mul(uint64_t a, uint64_t b)
+{
+    uint64_t hi = __umul64hi(a, b);
+    uint64_t lo = a * b;
+    return (hi << 1) | (lo >> 63);
+}
+
+template <int NP>
+__device__ __forceinline__ uint64_t energy_fx(const uint64_t *__restrict__ tfx, int tstride, const uint32_t *c)
+{
+    uint64_t e = __ldg(tfx + c[0]);
+#pragma unroll
+    for (int q = 1; q < NP; q++) e = fx_mul(e, __ldg(tfx + (size_t)q * tstride + c[q]));
+    return e;
+}
+
+template <int NP>
+__device__ __forceinline__ double energy_fp64(const double *__restrict__ t, int tstride, const uint32_t *c)
+{
+    double e = __ldg(t + c[0]);
+#pragma unroll
+    for (int q = 1; q < NP; q++) e = e * __ldg(t + (size_t)q * tstride + c[q]);
+    return e;
+}
+
+} // namespace rwnmr

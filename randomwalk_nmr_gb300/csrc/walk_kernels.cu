@@ -1,0 +1,600 @@
+// Walk kernels of the GB300 walker engine (sm_103a).
+//
+// Design (the reference's kernels, NMR_cpmg_cuda.cpp / NMR_pfgse_cuda.cpp, are one thread per
+// walker with FP64 energy per collision, a [16][walkers] FP64 energy buffer in HBM per launch and
+// host-finished reductions):
+//   * the hot loop is integer-only: position, xorshift64 state and per-phase collision counters
+//     live in registers; a walker's energy is never multiplied per collision. After each echo it
+//     is looked up as table[c] = round(f^c * 2^63) (the reference's FP64 repeated product f^c,
+//     rounded once to 64-bit fixed point). GB300 runs FP64 at a small fraction of its integer
+//     rate, so FP64 stays out of the per-step and per-echo paths;
+//   * per-echo sums are exact integers: each walker's 64-bit energy is split into three limbs
+//     (21/21/22 bits) and summed with warp-wide redux.sync, one lane per echo keeps the warp sum,
+//     warps combine in shared memory every 32 echoes and CTAs add into global 64-bit counters.
+//     Integer addition is associative, so results are bit-identical run to run and across launch
+//     shapes, and exact to 2^-63 per walker;
+//   * walker state is read once per launch and written once at its end; a launch covers a
+//     bounded number of echoes so that no single kernel runs for long on a shared GPU.
+#include <cstdint>
+#include <type_traits>
+#include <cuda_runtime.h>
+
+#include "walk_device.cuh"
+#include "walk_kernels.cuh"
+
+namespace rwnmr
+{
+
+namespace
+{
+constexpr unsigned FULL = 0xffffffffu;
+constexpr uint64_t M21 = (1ull << 21) - 1;
+
+template <int NP>
+struct WordsPerBlock
+{
+    static constexpr int value = NP == 1 ? 1 : (NP == 2 ? 2 : 4);
+};
+
+__device__ __forceinline__ void load_pos(const WalkState &s, int64_t i, WalkerPos &p, uint64_t &seed)
+{
+    p.x = s.x[i];
+    p.y = s.y[i];
+    p.z = s.z[i];
+    seed = s.seed[i];
+}
+} // namespace
+
+// ---------------------------------------------------------------------------------------------
+// CPMG / collision-mapping walk over echoes [e_begin, e_end).
+// acc layout: [(n_echoes+1)][K], K = 3 + NP: limbs of the energy sum after echo e (index e+1;
+// index 0 = initial state) and, for k = 3 + p, collisions on phase p gained during echo e.
+template <int BC, int NP>
+__global__ void __launch_bounds__(kWalkThreads) cpmg_walk_kernel(DevImage im, WalkState st, CpmgLaunch L)
+{
+    constexpr int W = WordsPerBlock<NP>::value;
+    constexpr int K = 3 + NP;
+    __shared__ unsigned long long sacc[32 * K];
+
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool active = i < st.n;
+
+    WalkerPos p{};
+    uint64_t seed = 0;
+    uint32_t c[NP];
+#pragma unroll
+    for (int q = 0; q < NP; q++) c[q] = 0;
+    if (active)
+    {
+        if (L.from_initial)
+        {
+            p.x = st.x0[i];
+            p.y = st.y0[i];
+            p.z = st.z0[i];
+            seed = st.seed0[i];
+        }
+        else
+        {
+            load_pos(st, i, p, seed);
+#pragma unroll
+            for (int q = 0; q < NP; q++) c[q] = st.coll[(size_t)q * st.n + i];
+        }
+        if (!start_ok<BC>(im, p))
+        {
+            atomicOr(L.status, kStatusBadStart);
+            active = false;
+        }
+        init_image_coords<BC>(im, p);
+    }
+
+    for (int k = threadIdx.x; k < 32 * K; k += blockDim.x) sacc[k] = 0;
+
+    uint64_t efx = (active && L.record) ? energy_fx<NP>(L.tfx, L.tstride, c) : 0;
+    if (L.record && L.e_begin == 0)
+    {
+        // initial energy sum (output index 0)
+        uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
+        uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((efx >> 21) & M21));
+        uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
+        if (lane == 0)
+        {
+            atomicAdd(&L.acc[0], (unsigned long long)r0);
+            atomicAdd(&L.acc[1], (unsigned long long)r1);
+            atomicAdd(&L.acc[2], (unsigned long long)r2);
+        }
+    }
+    __syncthreads();
+
+    for (int e0 = L.e_begin; e0 < L.e_end; e0 += 32)
+    {
+        const int e1 = min(e0 + 32, L.e_end);
+        uint32_t keep[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) keep[k] = 0;
+        for (int e = e0; e < e1; e++)
+        {
+            uint32_t gained[NP];
+#pragma unroll
+            for (int q = 0; q < NP; q++) gained[q] = 0;
+            if (active)
+            {
+                for (int s = 0; s < L.steps_per_echo; s++)
+                {
+                    bool wall;
+                    int ph;
+                    walker_step<BC, W>(im, p, seed, wall, ph);
+#pragma unroll
+                    for (int q = 0; q < NP; q++) gained[q] += (wall && ph == q) ? 1u : 0u;
+                }
+                bool changed = false;
+#pragma unroll
+                for (int q = 0; q < NP; q++)
+                {
+                    c[q] += gained[q];
+                    changed |= gained[q] != 0;
+                }
+                if (changed && L.record) efx = energy_fx<NP>(L.tfx, L.tstride, c);
+            }
+            if (L.record)
+            {
+                uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
+                uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((efx >> 21) & M21));
+                uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
+                const bool mine = lane == (e - e0);
+                keep[0] = mine ? r0 : keep[0];
+                keep[1] = mine ? r1 : keep[1];
+                keep[2] = mine ? r2 : keep[2];
+#pragma unroll
+                for (int q = 0; q < NP; q++)
+                {
+                    uint32_t rq = __reduce_add_sync(FULL, gained[q]);
+                    keep[3 + q] = mine ? rq : keep[3 + q];
+                }
+            }
+        }
+        if (L.record)
+        {
+            // lane l holds this warp's sums for echo e0 + l
+            if (lane < e1 - e0)
+            {
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    if (keep[k]) atomicAdd(&sacc[lane * K + k], (unsigned long long)keep[k]);
+            }
+            __syncthreads();
+            for (int k = threadIdx.x; k < (e1 - e0) * K; k += blockDim.x)
+            {
+                unsigned long long v = sacc[k];
+                if (v) atomicAdd(&L.acc[(size_t)(e0 + 1 + k / K) * K + (k % K)], v);
+                sacc[k] = 0;
+            }
+            __syncthreads();
+        }
+    }
+
+    if (active)
+    {
+        st.x[i] = p.x;
+        st.y[i] = p.y;
+        st.z[i] = p.z;
+        st.seed[i] = seed;
+#pragma unroll
+        for (int q = 0; q < NP; q++) st.coll[(size_t)q * st.n + i] = c[q];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Seed-replay adjoint of the CPMG echo sums with respect to the per-phase decrease factors.
+// A walker's energy is E = prod_q f_q^c_q, so dE/df_q = c_q f_q^(c_q - 1) prod_{r != q} f_r^c_r.
+// L.t holds [2][NP][tstride]: the energy tables f^k, then the derivative tables k f^(k-1). Each
+// walker replays its trajectory from its stored seed and accumulates sum_e g[e] dE(e)/df_q in FP64
+// (a few multiply-adds per walker-echo, no cross-lane FP64), then reduces once at the end.
+// partial: [gridDim.x][NP], summed on the host in block order (deterministic).
+template <int BC, int NP>
+__global__ void __launch_bounds__(kWalkThreads) cpmg_adjoint_kernel(DevImage im, WalkState st, AdjointLaunch L)
+{
+    constexpr int W = WordsPerBlock<NP>::value;
+    __shared__ double sred[kWalkThreads / 32][NP];
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    bool active = i < st.n;
+    WalkerPos p{};
+    uint64_t seed = 0;
+    uint32_t c[NP];
+    double acc[NP];
+#pragma unroll
+    for (int q = 0; q < NP; q++)
+    {
+        c[q] = 0;
+        acc[q] = 0.0;
+    }
+    if (active)
+    {
+        p.x = st.x0[i];
+        p.y = st.y0[i];
+        p.z = st.z0[i];
+        seed = st.seed0[i];
+        if (!start_ok<BC>(im, p))
+        {
+            atomicOr(L.status, kStatusBadStart);
+            active = false;
+        }
+        init_image_coords<BC>(im, p);
+    }
+    if (active)
+    {
+        const double *T = L.t;
+        const double *dT = L.t + (size_t)NP * L.tstride;
+        for (int e = 0; e < L.n_echoes; e++)
+        {
+            for (int s = 0; s < L.steps_per_echo; s++)
+            {
+                bool wall;
+                int ph;
+                walker_step<BC, W>(im, p, seed, wall, ph);
+#pragma unroll
+                for (int q = 0; q < NP; q++) c[q] += (wall && ph == q) ? 1u : 0u;
+            }
+            const double g = __ldg(L.grad + e + 1);
+            if (g != 0.0)
+            {
+                double tv[NP], dv[NP];
+#pragma unroll
+                for (int q = 0; q < NP; q++)
+                {
+                    tv[q] = __ldg(T + (size_t)q * L.tstride + c[q]);
+                    dv[q] = __ldg(dT + (size_t)q * L.tstride + c[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < NP; q++)
+                {
+                    double term = dv[q];
+#pragma unroll
+                    for (int r = 0; r < NP; r++)
+                        if (r != q) term *= tv[r];
+                    acc[q] = fma(g, term, acc[q]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NP; q++)
+    {
+        double v = acc[q];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+        if (lane == 0) sred[warp][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NP)
+    {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += sred[w][threadIdx.x];
+        L.partial[(size_t)blockIdx.x * NP + threadIdx.x] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// PFGSE walk: walkers walk cumulatively to each exposure time. At each one the kernel adds
+//   * the exact fixed-point energy sum (3 limbs) and the integer squared displacements per axis;
+//   * for a gradient along one axis (the usual case), each walker's fixed-point energy into a
+//     displacement histogram H_i[d] (two 32-bit-split limbs per bin), so the phase sums
+//     M_ij = sum_d H_i[d] cos(k_j d res) need one cosine per distinct displacement rather than
+//     one per walker (pfgse_phase_kernel);
+//   * for any other gradient direction, each walker's displacement and FP64 energy, measured by
+//     pfgse_direct_kernel.
+template <int BC, int NP>
+__global__ void __launch_bounds__(kWalkThreads) pfgse_walk_kernel(DevImage im, WalkState st, PfgseLaunch L)
+{
+    constexpr int W = WordsPerBlock<NP>::value;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool active = i < st.n;
+    WalkerPos p{};
+    uint64_t seed = 0;
+    int x0 = 0, y0 = 0, z0 = 0;
+    uint32_t c[NP];
+#pragma unroll
+    for (int q = 0; q < NP; q++) c[q] = 0;
+    if (active)
+    {
+        x0 = st.x0[i];
+        y0 = st.y0[i];
+        z0 = st.z0[i];
+        p.x = x0;
+        p.y = y0;
+        p.z = z0;
+        seed = st.seed0[i];
+        if (!start_ok<BC>(im, p))
+        {
+            atomicOr(L.status, kStatusBadStart);
+            active = false;
+        }
+        init_image_coords<BC>(im, p);
+    }
+    int done = 0;
+    for (int d = 0; d < L.n_delta; d++)
+    {
+        const int target = L.steps[d];
+        if (active)
+        {
+            for (; done < target; done++)
+            {
+                bool wall;
+                int ph;
+                walker_step<BC, W>(im, p, seed, wall, ph);
+#pragma unroll
+                for (int q = 0; q < NP; q++) c[q] += (wall && ph == q) ? 1u : 0u;
+            }
+        }
+        const uint64_t efx = active ? energy_fx<NP>(L.tfx, L.tstride, c) : 0ull;
+        const int ddx = p.x - x0, ddy = p.y - y0, ddz = p.z - z0;
+        unsigned long long *acc = L.acc + (size_t)d * 6;
+        uint32_t r;
+        r = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
+        if (lane == 0 && r) atomicAdd(&acc[0], (unsigned long long)r);
+        r = __reduce_add_sync(FULL, (uint32_t)((efx >> 21) & M21));
+        if (lane == 0 && r) atomicAdd(&acc[1], (unsigned long long)r);
+        r = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
+        if (lane == 0 && r) atomicAdd(&acc[2], (unsigned long long)r);
+        // squared displacements: |d| <= steps, so split at 16 bits to keep redux sums in 32 bits
+        const int dd[3] = {ddx, ddy, ddz};
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+        {
+            uint64_t sq = active ? (uint64_t)((int64_t)dd[a] * dd[a]) : 0ull;
+            uint32_t lo = __reduce_add_sync(FULL, (uint32_t)(sq & 0xffffull));
+            uint32_t hi = __reduce_add_sync(FULL, (uint32_t)(sq >> 16));
+            if (lane == 0 && (lo | hi)) atomicAdd(&acc[3 + a], (unsigned long long)lo + ((unsigned long long)hi << 16));
+        }
+        if (active)
+        {
+            if (L.axis >= 0)
+            {
+                const int dv = L.axis == 0 ? ddx : (L.axis == 1 ? ddy : ddz);
+                const int bin = dv + L.hist_half;
+                if ((unsigned)bin < (unsigned)(2 * L.hist_half + 1))
+                {
+                    unsigned long long *h = L.hist + ((size_t)d * (2 * L.hist_half + 1) + bin) * 2;
+                    atomicAdd(&h[0], (unsigned long long)(efx & 0xffffffffull));
+                    atomicAdd(&h[1], (unsigned long long)(efx >> 32));
+                }
+                else
+                {
+                    atomicOr(L.status, kStatusHistRange);
+                }
+            }
+            else
+            {
+                const size_t o = (size_t)d * st.n + i;
+                L.disp[o * 3 + 0] = ddx;
+                L.disp[o * 3 + 1] = ddy;
+                L.disp[o * 3 + 2] = ddz;
+                L.energy[o] = energy_fp64<NP>(L.t, L.tstride, c);
+            }
+        }
+    }
+    if (active)
+    {
+        st.x[i] = p.x;
+        st.y[i] = p.y;
+        st.z[i] = p.z;
+        st.seed[i] = seed;
+#pragma unroll
+        for (int q = 0; q < NP; q++) st.coll[(size_t)q * st.n + i] = c[q];
+    }
+}
+
+// M[i][j] (and optionally dM/dg) from the displacement histograms; one block per (i, j), bins in a
+// fixed order, so the result is deterministic.
+__global__ void pfgse_phase_kernel(PhaseLaunch L)
+{
+    const int i = blockIdx.y, j = blockIdx.x;
+    const int nb = 2 * L.hist_half + 1;
+    const double k = L.kaxis[j];
+    const unsigned long long *h = L.hist + (size_t)i * nb * 2;
+    double s = 0.0, g = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    {
+        const unsigned long long lo = h[2 * b], hi = h[2 * b + 1];
+        if ((lo | hi) == 0) continue;
+        // exact value hi * 2^32 + lo, scaled by 2^-63
+        const double e = ((double)hi * 4294967296.0 + (double)lo) * 1.0842021724855044e-19;
+        const double dd = (double)(b - L.hist_half);
+        const double arg = (k * dd) * L.res;
+        double sn, cs;
+        sincos(arg, &sn, &cs);
+        s += e * cs;
+        if (L.dMdg) g -= e * sn * (L.kscale_axis * dd * L.res);
+    }
+    __shared__ double red[2][256];
+    red[0][threadIdx.x] = s;
+    red[1][threadIdx.x] = g;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1)
+    {
+        if (threadIdx.x < o)
+        {
+            red[0][threadIdx.x] += red[0][threadIdx.x + o];
+            red[1][threadIdx.x] += red[1][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        L.M[(size_t)i * gridDim.x + j] = red[0][0];
+        if (L.dMdg) L.dMdg[(size_t)i * gridDim.x + j] = red[1][0];
+    }
+}
+
+// General gradient direction: per-walker cos((k_j . dR) res) E. Block partials, fixed-order
+// host-side finish: partial[(i * n_g + j) * gridDim.x + block].
+__global__ void pfgse_direct_kernel(DirectLaunch L)
+{
+    const int i = blockIdx.y;
+    double accs[kDirectMaxG];
+    double accg[kDirectMaxG];
+    const int ng = L.n_g;
+    for (int j = 0; j < ng; j++)
+    {
+        accs[j] = 0.0;
+        accg[j] = 0.0;
+    }
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < L.n; w += (int64_t)gridDim.x * blockDim.x)
+    {
+        const size_t o = (size_t)i * L.n + w;
+        const double dX = (double)L.disp[o * 3 + 0], dY = (double)L.disp[o * 3 + 1], dZ = (double)L.disp[o * 3 + 2];
+        const double e = L.energy[o];
+        for (int j = 0; j < ng; j++)
+        {
+            const double kd = L.kvec[3 * j] * dX + L.kvec[3 * j + 1] * dY + L.kvec[3 * j + 2] * dZ;
+            double sn, cs;
+            sincos(kd * L.res, &sn, &cs);
+            accs[j] += e * cs;
+            if (L.grad_on)
+            {
+                const double proj = L.kscale * (L.dir[0] * dX + L.dir[1] * dY + L.dir[2] * dZ);
+                accg[j] -= e * sn * proj * L.res;
+            }
+        }
+    }
+    __shared__ double red[256];
+    for (int j = 0; j < ng; j++)
+    {
+        for (int which = 0; which < (L.grad_on ? 2 : 1); which++)
+        {
+            red[threadIdx.x] = which ? accg[j] : accs[j];
+            __syncthreads();
+            for (int o = blockDim.x / 2; o > 0; o >>= 1)
+            {
+                if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+                __syncthreads();
+            }
+            if (threadIdx.x == 0)
+                (which ? L.partial_g : L.partial)[((size_t)i * ng + j) * gridDim.x + blockIdx.x] = red[0];
+            __syncthreads();
+        }
+    }
+}
+
+// Packs a label volume into bit-blocks with phase planes (BitBlock/bitBlock.cpp:138-221 plus the
+// multi-phase extension). One thread per block; voxels beyond the image edge stay pore.
+__global__ void pack_blocks_kernel(const uint8_t *__restrict__ labels, int nx, int ny, int nz, int bcols, int brows,
+                                   int64_t nblocks, int words, uint64_t *__restrict__ out, unsigned *status)
+{
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nblocks) return;
+    const int bx = (int)(b % bcols);
+    const int by = (int)((b / bcols) % brows);
+    const int bz = (int)(b / ((int64_t)bcols * brows));
+    uint64_t solid = 0, p0 = 0, p1 = 0, p2 = 0;
+    for (int k = 0; k < 64; k++)
+    {
+        const int x = bx * 4 + (k & 3), y = by * 4 + ((k >> 2) & 3), z = bz * 4 + (k >> 4);
+        if (x >= nx || y >= ny || z >= nz) continue;
+        const uint8_t l = labels[((int64_t)z * ny + y) * nx + x];
+        if (!l) continue;
+        solid |= 1ull << k;
+        const unsigned ph = (unsigned)l - 1u;
+        if (ph >= 8u) atomicOr(status, kStatusBadLabel);
+        p0 |= (uint64_t)(ph & 1u) << k;
+        p1 |= (uint64_t)((ph >> 1) & 1u) << k;
+        p2 |= (uint64_t)((ph >> 2) & 1u) << k;
+    }
+    uint64_t *o = out + b * words;
+    o[0] = solid;
+    if (words >= 2) o[1] = p0;
+    if (words >= 4)
+    {
+        o[2] = p1;
+        o[3] = p2;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Host-side dispatch over the (boundary condition, phase count) template grid.
+namespace
+{
+template <int NP, typename F>
+void with_bc(int bc_key, F &&f)
+{
+    switch (bc_key)
+    {
+    case BC_NOFLUX: f(std::integral_constant<int, BC_NOFLUX>{}); break;
+    case BC_PERIODIC: f(std::integral_constant<int, BC_PERIODIC>{}); break;
+    case BC_MIRROR: f(std::integral_constant<int, BC_MIRROR>{}); break;
+    default: f(std::integral_constant<int, BC_GENERIC>{}); break;
+    }
+}
+} // namespace
+
+cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkState &st, const CpmgLaunch &L,
+                             dim3 grid, cudaStream_t s)
+{
+    auto go = [&](auto npc) {
+        constexpr int NP = decltype(npc)::value;
+        with_bc<NP>(bc_key, [&](auto bcc) {
+            constexpr int BC = decltype(bcc)::value;
+            cpmg_walk_kernel<BC, NP><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+        });
+    };
+    if (np == 1) go(std::integral_constant<int, 1>{});
+    else if (np == 2) go(std::integral_constant<int, 2>{});
+    else go(std::integral_constant<int, 4>{});
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cpmg_adjoint(int bc_key, int np, const DevImage &im, const WalkState &st, const AdjointLaunch &L,
+                                dim3 grid, cudaStream_t s)
+{
+    auto go = [&](auto npc) {
+        constexpr int NP = decltype(npc)::value;
+        with_bc<NP>(bc_key, [&](auto bcc) {
+            constexpr int BC = decltype(bcc)::value;
+            cpmg_adjoint_kernel<BC, NP><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+        });
+    };
+    if (np == 1) go(std::integral_constant<int, 1>{});
+    else if (np == 2) go(std::integral_constant<int, 2>{});
+    else go(std::integral_constant<int, 4>{});
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pfgse_walk(int bc_key, int np, const DevImage &im, const WalkState &st, const PfgseLaunch &L,
+                              dim3 grid, cudaStream_t s)
+{
+    auto go = [&](auto npc) {
+        constexpr int NP = decltype(npc)::value;
+        with_bc<NP>(bc_key, [&](auto bcc) {
+            constexpr int BC = decltype(bcc)::value;
+            pfgse_walk_kernel<BC, NP><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+        });
+    };
+    if (np == 1) go(std::integral_constant<int, 1>{});
+    else if (np == 2) go(std::integral_constant<int, 2>{});
+    else go(std::integral_constant<int, 4>{});
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pfgse_phase(const PhaseLaunch &L, int n_delta, int n_g, cudaStream_t s)
+{
+    pfgse_phase_kernel<<<dim3(n_g, n_delta), 256, 0, s>>>(L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pfgse_direct(const DirectLaunch &L, int n_delta, int blocks, cudaStream_t s)
+{
+    pfgse_direct_kernel<<<dim3(blocks, n_delta), 256, 0, s>>>(L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_blocks(const uint8_t *labels, int nx, int ny, int nz, int bcols, int brows, int64_t nblocks,
+                               int words, uint64_t *out, unsigned *status, cudaStream_t s)
+{
+    const int t = 256;
+    pack_blocks_kernel<<<(unsigned)((nblocks + t - 1) / t), t, 0, s>>>(labels, nx, ny, nz, bcols, brows, nblocks,
+                                                                       words, out, status);
+    return cudaGetLastError();
+}
+
+} // namespace rwnmr

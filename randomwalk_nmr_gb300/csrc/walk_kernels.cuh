@@ -1,0 +1,107 @@
+// Launch-argument structs and launchers shared by walk_kernels.cu and engine.cu.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "walk_device.cuh"
+
+namespace rwnmr
+{
+
+constexpr int kWalkThreads = 256;
+constexpr int kDirectMaxG = 128; // gradient points handled by the general-direction PFGSE path
+
+// Device status word bits (the kernels never trap; they report through this word).
+constexpr unsigned kStatusBadStart = 1u;  // a walker started outside the image (noflux)
+constexpr unsigned kStatusHistRange = 2u; // a displacement fell outside the histogram
+constexpr unsigned kStatusBadLabel = 4u;  // a label exceeded the supported phase count
+
+// Walker state, structure of arrays. coll is [n_phases][n].
+struct WalkState
+{
+    int64_t n;
+    const int32_t *__restrict__ x0;
+    const int32_t *__restrict__ y0;
+    const int32_t *__restrict__ z0;
+    const uint64_t *__restrict__ seed0;
+    int32_t *x, *y, *z;
+    uint64_t *seed;
+    uint32_t *coll;
+};
+
+struct CpmgLaunch
+{
+    int e_begin, e_end;    // echoes walked by this launch
+    int steps_per_echo;
+    int from_initial;      // 1: start from (x0, seed0) with zero collisions; 0: continue (x, seed, coll)
+    int record;            // accumulate per-echo sums into acc
+    const uint64_t *tfx;   // [n_phases][tstride] fixed-point energy tables
+    int tstride;
+    unsigned long long *acc; // [(n_echoes+1)][3 + NP]
+    unsigned *status;
+};
+
+struct AdjointLaunch
+{
+    int n_echoes, steps_per_echo;
+    const double *t;     // [n_phases][tstride] FP64 energy tables
+    int tstride;
+    const double *grad;  // [n_echoes + 1]
+    double *partial;     // [gridDim.x][NP]
+    unsigned *status;
+};
+
+struct PfgseLaunch
+{
+    int n_delta;
+    const int32_t *steps;    // device [n_delta]
+    const uint64_t *tfx;
+    const double *t;
+    int tstride;
+    unsigned long long *acc; // [n_delta][6]: energy limbs x3, sum dx^2, dy^2, dz^2
+    int axis;                // gradient axis 0/1/2, or -1 for the general path
+    int hist_half;
+    unsigned long long *hist; // [n_delta][2*hist_half+1][2]
+    int32_t *disp;            // general path: [n_delta][n][3]
+    double *energy;           // general path: [n_delta][n]
+    unsigned *status;
+};
+
+struct PhaseLaunch
+{
+    const unsigned long long *hist;
+    int hist_half;
+    const double *kaxis; // device [n_g]
+    double res;
+    double kscale_axis;  // dk/dg along the axis (for dM/dg), 0 if unused
+    double *M;           // device [n_delta][n_g]
+    double *dMdg;        // device [n_delta][n_g] or null
+};
+
+struct DirectLaunch
+{
+    int64_t n;
+    int n_g;
+    const int32_t *disp;
+    const double *energy;
+    const double *kvec; // device [n_g][3]
+    double res;
+    int grad_on;
+    double kscale;
+    double dir[3];
+    double *partial;   // [n_delta][n_g][blocks]
+    double *partial_g; // [n_delta][n_g][blocks]
+};
+
+cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkState &st, const CpmgLaunch &L,
+                             dim3 grid, cudaStream_t s);
+cudaError_t launch_cpmg_adjoint(int bc_key, int np, const DevImage &im, const WalkState &st, const AdjointLaunch &L,
+                                dim3 grid, cudaStream_t s);
+cudaError_t launch_pfgse_walk(int bc_key, int np, const DevImage &im, const WalkState &st, const PfgseLaunch &L,
+                              dim3 grid, cudaStream_t s);
+cudaError_t launch_pfgse_phase(const PhaseLaunch &L, int n_delta, int n_g, cudaStream_t s);
+cudaError_t launch_pfgse_direct(const DirectLaunch &L, int n_delta, int blocks, cudaStream_t s);
+cudaError_t launch_pack_blocks(const uint8_t *labels, int nx, int ny, int nz, int bcols, int brows, int64_t nblocks,
+                               int words, uint64_t *out, unsigned *status, cudaStream_t s);
+
+} // namespace rwnmr

@@ -1,0 +1,246 @@
+"""Python binding of the GB300 walker engine's C ABI (include/rwnmr_gb300.h).
+
+The engine is the CUDA library ``_build/librwnmr_gb300.so``. There is no CPU fallback: if the
+library is missing or no CUDA device is usable, constructing an :class:`Engine` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+_vp = ctypes.c_void_p
+_LOCK = threading.Lock()
+_LIB = None
+
+BC = {"noflux": 0, "periodic": 1, "mirror": 2}
+
+STATUS = {
+    0: "RWNMR_OK",
+    1: "RWNMR_ERR_INVALID",
+    2: "RWNMR_ERR_CUDA",
+    3: "RWNMR_ERR_NOMEM",
+    4: "RWNMR_ERR_STATE",
+    5: "RWNMR_ERR_UNSUPPORTED",
+    6: "RWNMR_ERR_DEVICE",
+}
+
+# Every function the C header declares, for load checks.
+EXPORTS = [
+    "rwnmr_ctx_create", "rwnmr_ctx_destroy", "rwnmr_last_error", "rwnmr_version", "rwnmr_ctx_set_stream",
+    "rwnmr_ctx_launch_count", "rwnmr_ctx_last_kernel_ms", "rwnmr_image_upload", "rwnmr_image_upload_labels",
+    "rwnmr_image_download_blocks", "rwnmr_walkers_upload", "rwnmr_walkers_download", "rwnmr_cpmg_run",
+    "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
+]
+
+
+class RwnmrError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class CpmgParams(ctypes.Structure):
+    _fields_ = [
+        ("bc", ctypes.c_int32), ("shift", ctypes.c_int32), ("steps_per_echo", ctypes.c_int32),
+        ("n_echoes", ctypes.c_int32), ("dfactor", ctypes.POINTER(ctypes.c_double)),
+        ("echoes_per_launch", ctypes.c_int32),
+    ]
+
+
+class PfgseParams(ctypes.Structure):
+    _fields_ = [
+        ("bc", ctypes.c_int32), ("shift", ctypes.c_int32), ("n_delta", ctypes.c_int32),
+        ("steps", ctypes.POINTER(ctypes.c_int32)), ("n_g", ctypes.c_int32),
+        ("kvec", ctypes.POINTER(ctypes.c_double)), ("res", ctypes.c_double),
+        ("dfactor", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load_library(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Loads the engine library (building it first if asked and absent)."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = _build.LIB
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise FileNotFoundError(f"rwnmr_gb300 engine library not built: {path}")
+            _build.build()
+        lib = ctypes.CDLL(path)
+        lib.rwnmr_last_error.restype = ctypes.c_char_p
+        lib.rwnmr_last_error.argtypes = [_vp]
+        lib.rwnmr_version.restype = ctypes.c_char_p
+        lib.rwnmr_ctx_launch_count.restype = ctypes.c_int64
+        lib.rwnmr_ctx_launch_count.argtypes = [_vp]
+        lib.rwnmr_ctx_last_kernel_ms.restype = ctypes.c_double
+        lib.rwnmr_ctx_last_kernel_ms.argtypes = [_vp]
+        lib.rwnmr_ctx_destroy.argtypes = [_vp]
+        for name in EXPORTS:
+            getattr(lib, name)  # raises AttributeError if a declared symbol is missing
+        _LIB = lib
+        return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_vp)
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Engine:
+    """One rwnmr_ctx: an image, a walker population and the walks over them on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        ctx = _vp()
+        st = self.lib.rwnmr_ctx_create(ctypes.byref(ctx), int(device))
+        if st != 0:
+            raise RwnmrError(st, f"could not create a CUDA context on device {device}")
+        self.ctx = ctx
+        self.n_phases = 1
+        self.shape = None
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.rwnmr_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st != 0:
+            msg = self.lib.rwnmr_last_error(self.ctx)
+            raise RwnmrError(st, msg.decode() if msg else "")
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.rwnmr_ctx_launch_count(self.ctx))
+
+    @property
+    def last_kernel_ms(self) -> float:
+        return float(self.lib.rwnmr_ctx_last_kernel_ms(self.ctx))
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self.lib.rwnmr_ctx_set_stream(self.ctx, _vp(stream_ptr or 0)))
+
+    # -- image ------------------------------------------------------------------------------
+    def upload_labels(self, labels: np.ndarray, n_phases: int | None = None):
+        labels = np.ascontiguousarray(labels, dtype=np.uint8)
+        nz, ny, nx = labels.shape
+        if n_phases is None:
+            n_phases = max(1, int(labels.max()))
+        self._check(self.lib.rwnmr_image_upload_labels(self.ctx, _p(labels), nx, ny, nz, int(n_phases)))
+        self.n_phases = int(n_phases)
+        self.shape = (nz, ny, nx)
+
+    def upload_blocks(self, blocks: np.ndarray, shape, labels: np.ndarray | None = None, n_phases: int = 1):
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint64)
+        nz, ny, nx = shape
+        lab = None if labels is None else np.ascontiguousarray(labels, dtype=np.uint8)
+        self._check(self.lib.rwnmr_image_upload(self.ctx, _p(blocks), nx, ny, nz, _p(lab), int(n_phases)))
+        self.n_phases = int(n_phases)
+        self.shape = (nz, ny, nx)
+
+    def download_blocks(self) -> np.ndarray:
+        nz, ny, nx = self.shape
+        nb = ((nx + 3) // 4) * ((ny + 3) // 4) * ((nz + 3) // 4)
+        out = np.zeros(nb, np.uint64)
+        self._check(self.lib.rwnmr_image_download_blocks(self.ctx, _p(out)))
+        return out
+
+    # -- walkers ----------------------------------------------------------------------------
+    def upload_walkers(self, x0, y0, z0, seed0):
+        arrs = [np.ascontiguousarray(a, dtype=t) for a, t in
+                ((x0, np.int32), (y0, np.int32), (z0, np.int32), (seed0, np.uint64))]
+        n = len(arrs[0])
+        if any(len(a) != n for a in arrs):
+            raise ValueError("walker arrays differ in length")
+        self._check(self.lib.rwnmr_walkers_upload(self.ctx, ctypes.c_int64(n), *[_p(a) for a in arrs]))
+        self.n = n
+
+    def download_walkers(self):
+        n, P = self.n, self.n_phases
+        x, y, z = (np.zeros(n, np.int32) for _ in range(3))
+        s = np.zeros(n, np.uint64)
+        c = np.zeros((n, P), np.uint32)
+        self._check(self.lib.rwnmr_walkers_download(self.ctx, _p(x), _p(y), _p(z), _p(s), _p(c)))
+        return dict(x=x, y=y, z=z, seed=s, collisions=c)
+
+    def _dfactor(self, dfactor):
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(dfactor, np.float64), (self.n_phases,)))
+
+    # -- walks ------------------------------------------------------------------------------
+    def cpmg(self, n_echoes: int, steps_per_echo: int, dfactor, bc: str = "noflux", shift: int = 0,
+             echoes_per_launch: int = 0):
+        df = self._dfactor(dfactor)
+        prm = CpmgParams(BC[bc], int(shift), int(steps_per_echo), int(n_echoes), _dptr(df), int(echoes_per_launch))
+        echo_sum = np.zeros(n_echoes + 1)
+        echo_fx = np.zeros((n_echoes + 1, 3), np.uint64)
+        echo_coll = np.zeros((n_echoes, self.n_phases), np.uint64)
+        self._check(self.lib.rwnmr_cpmg_run(self.ctx, ctypes.byref(prm), _p(echo_sum), _p(echo_fx), _p(echo_coll)))
+        return dict(echo_sum=echo_sum, echo_fx=echo_fx, echo_coll=echo_coll)
+
+    def cpmg_adjoint(self, n_echoes: int, steps_per_echo: int, dfactor, grad_echo, bc: str = "noflux",
+                     shift: int = 0):
+        df = self._dfactor(dfactor)
+        prm = CpmgParams(BC[bc], int(shift), int(steps_per_echo), int(n_echoes), _dptr(df), 0)
+        g = np.ascontiguousarray(grad_echo, np.float64)
+        if g.shape != (n_echoes + 1,):
+            raise ValueError("grad_echo must have n_echoes + 1 entries")
+        out = np.zeros(self.n_phases)
+        self._check(self.lib.rwnmr_cpmg_adjoint(self.ctx, ctypes.byref(prm), _p(g), _p(out)))
+        return out
+
+    def map(self, steps: int, bc: str = "noflux", shift: int = 0) -> np.ndarray:
+        out = np.zeros(self.n, np.uint32)
+        self._check(self.lib.rwnmr_map_run(self.ctx, BC[bc], int(shift), ctypes.c_int64(steps), _p(out)))
+        return out
+
+    def _pfgse_params(self, steps, kvec, res, dfactor, bc, shift):
+        steps = np.ascontiguousarray(steps, np.int32)
+        kvec = np.ascontiguousarray(kvec, np.float64).reshape(-1, 3)
+        df = self._dfactor(dfactor)
+        prm = PfgseParams(BC[bc], int(shift), len(steps), steps.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                          len(kvec), _dptr(kvec), float(res), _dptr(df))
+        return prm, (steps, kvec, df)
+
+    def pfgse(self, steps, kvec, res: float, dfactor, bc: str = "noflux", shift: int = 0):
+        prm, keep = self._pfgse_params(steps, kvec, res, dfactor, bc, shift)
+        nd, ng = prm.n_delta, prm.n_g
+        M = np.zeros((nd, ng))
+        esum = np.zeros(nd)
+        msd = np.zeros((nd, 3), np.uint64)
+        self._check(self.lib.rwnmr_pfgse_run(self.ctx, ctypes.byref(prm), _p(M), _p(esum), _p(msd)))
+        return dict(M=M, esum=esum, msd=msd)
+
+    def pfgse_grad_g(self, steps, kvec, res: float, dfactor, kscale: float, direction, bc="noflux", shift=0):
+        prm, keep = self._pfgse_params(steps, kvec, res, dfactor, bc, shift)
+        d = np.ascontiguousarray(direction, np.float64)
+        out = np.zeros((prm.n_delta, prm.n_g))
+        self._check(self.lib.rwnmr_pfgse_grad_g(self.ctx, ctypes.byref(prm), ctypes.c_double(kscale), _p(d), _p(out)))
+        return out
+
+
+def fx_to_float(limbs) -> np.ndarray:
+    """Exact fixed-point limb sums ([..., 3], scale 2^63) to float64."""
+    limbs = np.asarray(limbs, dtype=np.uint64)
+    flat = limbs.reshape(-1, 3)
+    vals = [(int(a) + (int(b) << 21) + (int(c) << 42)) / float(1 << 63) for a, b, c in flat]
+    return np.array(vals).reshape(limbs.shape[:-1])

@@ -1,0 +1,67 @@
+"""The seed-replay adjoint kernel against (1) an FP64 CPU pathwise gradient built from the
+oracle's per-walker collision histories and (2) central finite differences under common random
+numbers (same seeds, so the trajectories are fixed and the echo train is smooth in f)."""
+import numpy as np
+import pytest
+
+from conftest import dfactor
+from randomwalk_nmr_gb300 import host
+
+pytestmark = pytest.mark.gpu
+
+
+def setup(engine, n_phases, seed=12, n=3000):
+    lab, _ = host.synth_spheres((24, 28, 22), 2.0, 5.0, 0.4, n_phases, seed=seed)
+    blocks, _ = host.pack_blocks(lab)
+    x, y, z, s, _ = host.place_walkers(blocks, lab.shape, n, seed)
+    engine.upload_labels(lab, n_phases)
+    engine.upload_walkers(x, y, z, s)
+    return lab, (x, y, z, s)
+
+
+def pathwise_gradient(oracle, lab, w, n_echoes, spe, f, grad, n_phases):
+    """sum_e g_e sum_w dE_w(e)/df_q from per-walker, per-echo collision counts (CPU, FP64)."""
+    f = np.asarray(f, np.float64)
+    P = n_phases
+    counts = np.zeros((n_echoes + 1, len(w[0]), P), np.int64)
+    state = [np.array(a) for a in w]
+    for e in range(n_echoes):
+        o = oracle.cpmg(lab, tuple(state), 1, spe, f, n_phases=n_phases, threads=4)
+        counts[e + 1] = counts[e] + o["collf"].astype(np.int64)
+        state = [o["xf"], o["yf"], o["zf"], o["seedf"]]
+    out = np.zeros(P)
+    for q in range(P):
+        c = counts[..., q].astype(np.float64)
+        dq = np.where(c > 0, c * f[q] ** np.maximum(c - 1, 0), 0.0)
+        other = np.ones_like(c)
+        for r in range(P):
+            if r != q:
+                other *= f[r] ** counts[..., r]
+        out[q] = np.sum(grad[:, None] * dq * other)
+    return out
+
+
+@pytest.mark.parametrize("n_phases", [1, 2])
+def test_adjoint_matches_pathwise_and_finite_differences(engine, oracle, n_phases):
+    lab, w = setup(engine, n_phases)
+    n_echoes, spe = 60, 2
+    f = dfactor([10.0, 30.0][:n_phases])
+    rng = np.random.default_rng(0)
+    grad = rng.normal(size=n_echoes + 1)
+    adj = engine.cpmg_adjoint(n_echoes, spe, f, grad)
+    ref = pathwise_gradient(oracle, lab, w, n_echoes, spe, f, grad, n_phases)
+    np.testing.assert_allclose(adj, ref, rtol=1e-10)
+    h = 1e-6
+    for q in range(n_phases):
+        fp, fm = f.copy(), f.copy()
+        fp[q] += h
+        fm[q] -= h
+        Lp = grad @ engine.cpmg(n_echoes, spe, fp)["echo_sum"]
+        Lm = grad @ engine.cpmg(n_echoes, spe, fm)["echo_sum"]
+        np.testing.assert_allclose(adj[q], (Lp - Lm) / (2 * h), rtol=1e-5)
+
+
+def test_adjoint_zero_gradient_is_zero(engine):
+    setup(engine, 1)
+    adj = engine.cpmg_adjoint(20, 1, dfactor(10.0), np.zeros(21))
+    assert np.all(adj == 0.0)

@@ -1,0 +1,154 @@
+"""GPU parity of the CPMG / mapping walk against the CPU oracle (bit-exact integers, exact
+fixed-point echo sums, FP64 echo sums within 1e-12 relative of the oracle's serial FP64 sum)."""
+import numpy as np
+import pytest
+
+from conftest import dfactor
+from randomwalk_nmr_gb300 import fx_to_float, host
+
+pytestmark = pytest.mark.gpu
+
+# echo amplitudes: GPU fixed-point sum vs the oracle's serial FP64 sum of the same energies
+ECHO_RTOL = 1e-12
+
+
+def image(shape=(26, 22, 30), seed=3, porosity=0.35, n_phases=1, rmin=2.0, rmax=6.0):
+    lab, _ = host.synth_spheres(shape, rmin, rmax, porosity, n_phases, seed=seed)
+    return lab
+
+
+def walkers(lab, n, seed, shift=0, mode="random", dev=0):
+    blocks, _ = host.pack_blocks(lab)
+    x, y, z, s, info = host.place_walkers(blocks, lab.shape, n, seed, mode, dev, shift)
+    return x, y, z, s
+
+
+def run_both(engine, oracle, lab, w, n_echoes, spe, df, bc="noflux", shift=0, n_phases=None, chunk=0):
+    engine.upload_labels(lab, n_phases)
+    engine.upload_walkers(*w)
+    g = engine.cpmg(n_echoes, spe, df, bc=bc, shift=shift, echoes_per_launch=chunk)
+    st = engine.download_walkers()
+    o = oracle.cpmg(lab, w, n_echoes, spe, df, bc=bc, shift=shift, n_phases=n_phases, threads=4)
+    return g, st, o
+
+
+def assert_parity(g, st, o):
+    assert np.array_equal(st["x"], o["xf"])
+    assert np.array_equal(st["y"], o["yf"])
+    assert np.array_equal(st["z"], o["zf"])
+    assert np.array_equal(st["seed"], o["seedf"])
+    assert np.array_equal(st["collisions"], o["collf"])
+    assert np.array_equal(g["echo_coll"], o["echo_coll"])
+    assert np.array_equal(g["echo_fx"], o["echo_fx"])
+    np.testing.assert_allclose(g["echo_sum"], o["echo_fp64"], rtol=ECHO_RTOL, atol=0)
+    np.testing.assert_allclose(g["echo_sum"], fx_to_float(g["echo_fx"]), rtol=1e-15)
+
+
+@pytest.mark.parametrize("bc", ["noflux", "periodic", "mirror"])
+@pytest.mark.parametrize("shift", [0, 1])
+def test_cpmg_parity_bc_shift(engine, oracle, bc, shift):
+    lab = image()
+    w = walkers(lab, 3000, 7, shift=shift)
+    g, st, o = run_both(engine, oracle, lab, w, 150, 2, dfactor(10.0), bc=bc, shift=shift)
+    assert_parity(g, st, o)
+
+
+@pytest.mark.parametrize("n_phases", [2, 3, 4])
+def test_cpmg_parity_multiphase(engine, oracle, n_phases):
+    lab = image(n_phases=n_phases, seed=11)
+    w = walkers(lab, 2000, 5)
+    rho = [5.0, 25.0, 12.0, 40.0][:n_phases]
+    g, st, o = run_both(engine, oracle, lab, w, 120, 3, dfactor(rho), n_phases=n_phases)
+    assert_parity(g, st, o)
+    assert np.all(g["echo_coll"].sum(axis=0) > 0)
+
+
+def test_cpmg_parity_reference_golden(engine, golden):
+    """Against the reference's own per-echo walk outputs."""
+    gd = golden
+    lab = gd["img_a"]
+    w = (gd["walk_x0"], gd["walk_y0"], gd["walk_z0"], gd["walk_seed0"])
+    engine.upload_labels(lab)
+    engine.upload_walkers(*w)
+    g = engine.cpmg(200, 2, float(gd["walk_dfactor"][0]))
+    st = engine.download_walkers()
+    assert np.array_equal(st["x"], gd["walk_xf"])
+    assert np.array_equal(st["y"], gd["walk_yf"])
+    assert np.array_equal(st["z"], gd["walk_zf"])
+    assert np.array_equal(st["seed"], gd["walk_seedf"])
+    assert np.array_equal(st["collisions"][:, 0], gd["walk_coll"])
+    assert np.array_equal(g["echo_coll"][:, 0], gd["walk_coll_per_echo"])
+    np.testing.assert_allclose(g["echo_sum"], gd["walk_energy_sum"], rtol=ECHO_RTOL)
+
+
+def test_cpmg_launch_chunking_is_invisible(engine, oracle):
+    lab = image(seed=5)
+    w = walkers(lab, 1500, 3)
+    outs = []
+    for chunk in (0, 7, 32, 500):
+        engine.upload_labels(lab)
+        engine.upload_walkers(*w)
+        outs.append(engine.cpmg(257, 1, dfactor(30.0), echoes_per_launch=chunk))
+    for o in outs[1:]:
+        assert np.array_equal(o["echo_fx"], outs[0]["echo_fx"])
+        assert np.array_equal(o["echo_coll"], outs[0]["echo_coll"])
+
+
+def test_cpmg_deterministic_and_rerunnable(engine):
+    lab = image(seed=9)
+    w = walkers(lab, 4000, 1)
+    engine.upload_labels(lab)
+    engine.upload_walkers(*w)
+    a = engine.cpmg(100, 2, dfactor(10.0))
+    b = engine.cpmg(100, 2, dfactor(10.0))
+    assert np.array_equal(a["echo_fx"], b["echo_fx"])
+    assert np.array_equal(a["echo_sum"], b["echo_sum"])
+
+
+def test_cpmg_edge_cases(engine, oracle):
+    lab = image(shape=(5, 7, 9), seed=2, porosity=0.6, rmin=1.0, rmax=2.0)
+    # walkers on every face of the image
+    zz, yy, xx = np.nonzero(lab == 0)
+    on_face = (xx == 0) | (yy == 0) | (zz == 0) | (xx == 8) | (yy == 6) | (zz == 4)
+    idx = np.nonzero(on_face)[0]
+    w = (xx[idx].astype(np.int32), yy[idx].astype(np.int32), zz[idx].astype(np.int32),
+         np.arange(1, len(idx) + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15))
+    for bc in ("noflux", "periodic", "mirror"):
+        g, st, o = run_both(engine, oracle, lab, w, 64, 5, dfactor(20.0), bc=bc)
+        assert_parity(g, st, o)
+    # zero echoes, zero walkers
+    engine.upload_walkers(*w)
+    z = engine.cpmg(0, 1, dfactor(20.0))
+    assert z["echo_sum"][0] == len(idx)
+    engine.upload_walkers(*(a[:0] for a in w))
+    e = engine.cpmg(10, 1, dfactor(20.0))
+    assert np.all(e["echo_sum"] == 0) and np.all(e["echo_coll"] == 0)
+
+
+def test_cpmg_rejects_bad_input(engine):
+    from randomwalk_nmr_gb300 import RwnmrError
+
+    lab = image()
+    engine.upload_labels(lab)
+    with pytest.raises(RwnmrError):
+        engine.cpmg(10, 1, 0.5)  # walkers missing
+    engine.upload_walkers(np.array([500], np.int32), np.array([0], np.int32), np.array([0], np.int32),
+                          np.array([1], np.uint64))
+    with pytest.raises(RwnmrError, match="outside the image"):
+        engine.cpmg(10, 1, 0.5)
+    with pytest.raises(RwnmrError):
+        engine.cpmg(10, 1, 1.5)  # decrease factor outside [0, 1]
+
+
+@pytest.mark.parametrize("bc", ["noflux", "periodic"])
+def test_map_walk_matches_oracle(engine, oracle, bc):
+    lab = image(seed=4)
+    w = walkers(lab, 2500, 8)
+    engine.upload_labels(lab)
+    engine.upload_walkers(*w)
+    coll = engine.map(20000 + 17, bc=bc)
+    d, oc = oracle.displacements(lab, w, 20000 + 17, bc=bc, threads=4)
+    assert np.array_equal(coll, oc[:, 0])
+    st = engine.download_walkers()
+    assert np.array_equal(st["x"] - w[0], d[0])
+    assert np.array_equal(st["z"] - w[2], d[2])
