@@ -115,6 +115,40 @@ rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, double *
 rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, const double *grad_echo,
                                 double *grad_dfactor);
 
+/* ---- CPMG walk without allocation ------------------------------------------------------ */
+/* No counterpart in the reference (its CUDA path cudaMallocs its buffers on every run).
+ * For callers that cannot let a library allocate device memory -- a framework whose caching
+ * allocator owns the GPU's memory under a fixed budget, or an application under a hard
+ * device-memory cap that pre-allocates everything -- this entry point takes device pointers for
+ * all inputs and outputs and allocates nothing: no context, no cudaMalloc/cudaFree. Its scratch
+ * (energy tables, per-echo accumulators, status word) lives in one file-scope device array of
+ * 8 MiB that every GPU loading the library holds until exit; walks whose tables and accumulators
+ * need more than that are rejected with RWNMR_ERR_UNSUPPORTED. All calls on a device share that
+ * array: each call clears what it uses, but calls that overlap on the GPU race and must be
+ * serialised by the caller. The first call on a device resolves the array's address with that
+ * device current; make it before any stream capture. Runs on `stream` and synchronises it before
+ * returning. Results equal rwnmr_cpmg_run's (echo_sum to the last bits of FP64 rounding). */
+typedef struct rwnmr_noalloc_cpmg_args
+{
+    const uint64_t *blocks;    /* device: bit-blocks, 1 word per block for one phase; for n_phases
+                                  2 (or 3-4) blocks of 2 (or 4) words: solid mask, then bit-planes
+                                  of the solid voxel's phase index (label - 1) */
+    int32_t nx, ny, nz, n_phases;
+    int64_t n;                 /* walkers */
+    const int32_t *x0, *y0, *z0; /* device: initial positions */
+    const uint64_t *seed0;     /* device: initial RNG states */
+    int32_t *x, *y, *z;        /* device out: final positions */
+    uint64_t *seed;            /* device out: final RNG states */
+    uint32_t *collisions;      /* device out: [n_phases][n] collision totals */
+    double *echo_sum;          /* device out: [n_echoes+1] */
+    unsigned long long *echo_coll; /* device out, nullable: [n_echoes][n_phases] */
+    void *stream;              /* cudaStream_t, NULL = legacy default stream */
+} rwnmr_noalloc_cpmg_args;
+
+/* err (nullable, errlen bytes) receives a message on failure. */
+rwnmr_status rwnmr_cpmg_run_noalloc(const rwnmr_cpmg_params *p, const rwnmr_noalloc_cpmg_args *args, char *err,
+                                    int errlen);
+
 /* ---- collision-mapping walk ------------------------------------------------------------ */
 /* NMR_Simulation::mapSimulation (NMR_Simulation.cpp:1787-1841; NMR_Simulation_cuda.cpp:726-1270):
  * walks every walker from its initial state for `steps` steps and writes its collision count. */
