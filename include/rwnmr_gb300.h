@@ -153,6 +153,10 @@ rwnmr_status rwnmr_cpmg_run_noalloc(const rwnmr_cpmg_params *p, const rwnmr_noal
 /* NMR_Simulation::mapSimulation (NMR_Simulation.cpp:1787-1841; NMR_Simulation_cuda.cpp:726-1270):
  * walks every walker from its initial state for `steps` steps and writes its collision count. */
 rwnmr_status rwnmr_map_run(rwnmr_ctx *ctx, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions);
+/* Same walk continued from the state the previous walk left (positions, RNG states, collision
+ * totals), as the reference's histogram windows continue one another (NMR_Simulation.cpp:1787-1841);
+ * collisions receives the running totals. */
+rwnmr_status rwnmr_map_continue(rwnmr_ctx *ctx, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions);
 
 /* ---- PFGSE walk ------------------------------------------------------------------------ */
 typedef struct rwnmr_pfgse_params

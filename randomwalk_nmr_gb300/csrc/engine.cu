@@ -544,7 +544,21 @@ rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const 
 }
 
 // ---- collision mapping ------------------------------------------------------------------------
+static rwnmr_status map_impl(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions,
+                             bool from_initial);
+
 rwnmr_status rwnmr_map_run(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions)
+{
+    return map_impl(c, bc, shift, steps, collisions, true);
+}
+
+rwnmr_status rwnmr_map_continue(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions)
+{
+    return map_impl(c, bc, shift, steps, collisions, false);
+}
+
+static rwnmr_status map_impl(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions,
+                             bool from_initial)
 {
     RW_TRY(need_run_state(c));
     RW_TRY(check_geom(c, bc, shift));
@@ -566,7 +580,7 @@ rwnmr_status rwnmr_map_run(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t step
         {
             L.e_begin = 0;
             L.e_end = 0;
-            L.from_initial = 1;
+            L.from_initial = from_initial ? 1 : 0;
             L.steps_per_echo = 1;
             RW_CUDA(c, launch_cpmg_walk(bc_key(bc, shift), slots, im, st, L, walk_grid(c->n), c->stream), "map kernel");
             c->launches++;
@@ -576,7 +590,7 @@ rwnmr_status rwnmr_map_run(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t step
             L.e_begin = 0;
             L.e_end = 1;
             L.steps_per_echo = (int)std::min<int64_t>(chunk, steps - s);
-            L.from_initial = s == 0;
+            L.from_initial = (s == 0 && from_initial) ? 1 : 0;
             RW_CUDA(c, launch_cpmg_walk(bc_key(bc, shift), slots, im, st, L, walk_grid(c->n), c->stream), "map kernel");
             c->launches++;
         }

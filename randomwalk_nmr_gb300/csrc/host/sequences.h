@@ -1,0 +1,127 @@
+// Host-side simulation and sequences: the reference's NMR_Simulation / NMR_cpmg / NMR_PFGSE
+// orchestration (config -> image -> walkers -> walk -> outputs), with every walk on the GPU engine.
+#pragma once
+#include <cstdint>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "config.h"
+#include "rwnmr_gb300.h"
+
+namespace rwnmr_host
+{
+
+struct Image
+{
+    int nx = 0, ny = 0, nz = 0, n_phases = 1;
+    std::vector<uint8_t> labels; // [nz][ny][nx], 0 = pore, p = solid phase p
+    std::vector<uint64_t> blocks;
+    std::string source;
+};
+
+// Loads the image slices named by a uct config (PNG; any non-zero colour channel is solid, as in
+// NMR_Simulation::createBinaryMap, NMR_Simulation.cpp:577-617).
+bool load_uct_image(const UctConfig &uct, Image &img, std::string &err);
+// Decodes one 8-bit PNG into a solid/pore mask (1 = solid). Non-interlaced PNGs, any colour type.
+bool png_solid_mask(const std::string &path, int &width, int &height, std::vector<uint8_t> &mask, std::string &err);
+
+// xi-rate collision histogram (NMR_Simulation/CollisionHistogram.cpp:59-249).
+struct Histogram
+{
+    int size = 0;
+    double gap = 0.0;
+    std::string scale = "linear";
+    int first_echo = 0, last_echo = 0;
+    std::vector<double> bins, amps;
+    void create(int size, const std::string &scale);
+    void fill(const std::vector<uint32_t> &collisions, uint32_t steps);
+};
+
+class Simulation
+{
+  public:
+    RwnmrConfig rw;
+    UctConfig uct;
+    std::string db_path, sim_dir;
+    std::mt19937 rng;
+    uint64_t initial_seed = 0;
+    Image img;
+    double resolution = 1.0, voxel_res = 1.0, dt = 0.0, gamma = 0.0;
+    int shift = 0;
+    bool voxel_division_applied = false;
+    uint32_t pores = 0, interface_count = 0, clamped = 0;
+    double porosity = 0.0, svp = 0.0, occupancy = 0.0;
+    std::vector<int32_t> x0, y0, z0;
+    std::vector<uint64_t> seed0;
+    std::vector<double> rho_phase; // relaxivity per solid phase
+    uint32_t steps = 0, echoes = 0;
+    std::vector<uint32_t> collisions;
+    std::vector<double> xi_rate;
+    Histogram histogram;
+    std::vector<Histogram> hist_list;
+    rwnmr_ctx *ctx = nullptr;
+    int device = 0;
+    bool quiet = false;
+
+    ~Simulation();
+    // NMR_Simulation constructor (NMR_Simulation.cpp:44-108)
+    bool init(const RwnmrConfig &rw, const UctConfig &uct, const std::string &project_root, int device,
+              std::string &err);
+    // readImage's bookkeeping after loading (pores, S/Vp) and the upload to the GPU
+    bool set_image(Image &&image, std::string &err);
+    // setWalkers (NMR_Simulation.cpp:324-409) and the upload to the GPU
+    bool set_walkers(std::string &err);
+    void set_time_framework_time(double time_ms); // NMR_Simulation.cpp:285-298
+    void set_time_framework_steps(uint32_t steps);
+    // collision-mapping walk with histogram windows (mapSimulation, NMR_Simulation.cpp:1787-1841)
+    bool map_simulation(std::string &err);
+    double decrease_factor(double rho) const; // Walker::computeDecreaseFactor
+    std::vector<double> phase_dfactors() const;
+    int bc_code() const;
+    void save_info() const;
+    void log(const std::string &msg) const;
+};
+
+class CpmgSequence
+{
+  public:
+    Simulation &sim;
+    CpmgConfig cfg;
+    std::string name, dir;
+    std::vector<double> times, amps, raw, noise;
+    std::vector<uint64_t> echo_collisions; // [echoes][phases]
+    double kernel_ms = 0.0;
+    CpmgSequence(Simulation &s, const CpmgConfig &c) : sim(s), cfg(c) {}
+    bool run(std::string &err); // set + run_simulation + save (NMR_cpmg::run, NMR_cpmg.cpp:87-93)
+    bool set(std::string &err);
+    bool run_simulation(std::string &err);
+    void save() const;
+};
+
+class PfgseSequence
+{
+  public:
+    Simulation &sim;
+    PfgseConfig cfg;
+    std::string dir;
+    std::vector<double> exposure_times;
+    std::vector<double> gradient;        // |g_j|
+    std::vector<double> gvec, kvec;      // [n_g][3]
+    int n_g = 0;
+    // per exposure time
+    std::vector<double> Mkt;             // [n_delta][n_g] un-normalised (sum E cos), after bulk and noise
+    std::vector<double> esum, dsat, dsat_err, dmsd;
+    std::vector<int> dsat_points;
+    std::vector<double> msd_vec, dmsd_vec; // [n_delta][3]
+    std::vector<double> lhs, rhs, raw_noise; // [n_delta][n_g]
+    std::vector<uint32_t> steps;
+    double kernel_ms = 0.0;
+    PfgseSequence(Simulation &s, const PfgseConfig &c) : sim(s), cfg(c) {}
+    bool run(std::string &err); // NMR_PFGSE::run (NMR_pfgse.cpp:98-131)
+};
+
+// The RWNMR command line (Utils/ArgsParser.cpp:10-152, App/rwnmrApp.cpp:106-231).
+int cli_main(int argc, const char *const *argv);
+
+} // namespace rwnmr_host

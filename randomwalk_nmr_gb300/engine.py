@@ -34,7 +34,8 @@ EXPORTS = [
     "rwnmr_ctx_create", "rwnmr_ctx_destroy", "rwnmr_last_error", "rwnmr_version", "rwnmr_ctx_set_stream",
     "rwnmr_ctx_launch_count", "rwnmr_ctx_last_kernel_ms", "rwnmr_image_upload", "rwnmr_image_upload_labels",
     "rwnmr_image_download_blocks", "rwnmr_walkers_upload", "rwnmr_walkers_download", "rwnmr_cpmg_run",
-    "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
+    "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_map_continue", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
+    "rwnmr_cpmg_run_noalloc",
 ]
 
 
@@ -211,6 +212,11 @@ class Engine:
     def map(self, steps: int, bc: str = "noflux", shift: int = 0) -> np.ndarray:
         out = np.zeros(self.n, np.uint32)
         self._check(self.lib.rwnmr_map_run(self.ctx, BC[bc], int(shift), ctypes.c_int64(steps), _p(out)))
+        return out
+
+    def map_continue(self, steps: int, bc: str = "noflux", shift: int = 0) -> np.ndarray:
+        out = np.zeros(self.n, np.uint32)
+        self._check(self.lib.rwnmr_map_continue(self.ctx, BC[bc], int(shift), ctypes.c_int64(steps), _p(out)))
         return out
 
     def _pfgse_params(self, steps, kvec, res, dfactor, bc, shift):

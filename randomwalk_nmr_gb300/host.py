@@ -10,7 +10,8 @@ from .engine import load_library
 
 _vp = ctypes.c_void_p
 
-HOST_EXPORTS = ["rwnmr_synth_spheres", "rwnmr_pack_blocks", "rwnmr_place_walkers"]
+HOST_EXPORTS = ["rwnmr_synth_spheres", "rwnmr_pack_blocks", "rwnmr_place_walkers", "rwnmr_png_solid_mask",
+                "rwnmr_config_json", "rwnmr_cli_main"]
 
 
 class PlacementInfo(ctypes.Structure):
@@ -23,6 +24,7 @@ def _lib():
     L.rwnmr_synth_spheres.restype = ctypes.c_int64
     L.rwnmr_pack_blocks.restype = ctypes.c_int64
     L.rwnmr_place_walkers.restype = ctypes.c_int
+    L.rwnmr_png_solid_mask.restype = ctypes.c_int64
     return L
 
 
@@ -69,3 +71,32 @@ def place_walkers(blocks: np.ndarray, shape, n: int, seed: int, mode: str = "ran
         raise ValueError(f"walker placement failed (rc={rc})")
     return x0, y0, z0, s0, dict(pores=info.pores, porosity=info.porosity, occupancy=info.occupancy,
                                 clamped=info.clamped)
+
+
+def png_mask(path: str) -> np.ndarray:
+    """Solid mask [height][width] of one PNG slice (1 = solid)."""
+    L = _lib()
+    w, h = ctypes.c_int32(), ctypes.c_int32()
+    err = ctypes.create_string_buffer(512)
+    n = L.rwnmr_png_solid_mask(path.encode(), ctypes.byref(w), ctypes.byref(h), None, err, len(err))
+    if n < 0:
+        raise ValueError(err.value.decode())
+    out = np.zeros((h.value, w.value), np.uint8)
+    L.rwnmr_png_solid_mask(path.encode(), None, None, _p(out), err, len(err))
+    return out
+
+
+def cli(args, cwd=None) -> int:
+    """Runs the command-line driver in-process (argv without the program name)."""
+    import os
+
+    L = _lib()
+    argv = [b"rwnmr_gb300"] + [str(a).encode() for a in args]
+    arr = (ctypes.c_char_p * len(argv))(*argv)
+    old = os.getcwd()
+    try:
+        if cwd:
+            os.chdir(cwd)
+        return int(L.rwnmr_cli_main(len(argv), arr))
+    finally:
+        os.chdir(old)

@@ -1,0 +1,97 @@
+"""The command-line driver end to end (config files -> image -> walkers -> GPU walk -> output
+files), checked against the reference's own CPU sequences on the same inputs (golden fixtures)."""
+import os
+
+import numpy as np
+import pytest
+
+from randomwalk_nmr_gb300 import host
+
+pytestmark = pytest.mark.gpu
+
+
+def write(path, text):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, "w") as f:
+        f.write(text)
+
+
+RW = ("NAME: t\nD0: 2.5\nBULK_TIME: {bulk}\nRHO_TYPE: uniform\nRHO: {{{rho}}}\nWALKERS: {n}\n"
+      "WALKERS_PLACEMENT: random\nSTEPS_PER_ECHO: {spe}\nSEED: {seed}\nBC: noflux\n"
+      "GIROMAGNETIC_RATIO: 42.576\nGIROMAGNETIC_UNIT: mhertz\nHISTOGRAMS: 1\nHISTOGRAM_SIZE: 1024\n")
+IMG_A = "24,20,28,2,6,0.35,1,3"  # the sphere pack of the golden fixtures (nx, ny, nz, rmin, rmax, porosity, phases, seed)
+
+
+def test_cli_cpmg_matches_reference_sequence(tmp_path, golden):
+    root = str(tmp_path / "config") + "/"
+    write(root + "default/rwnmr.config", RW.format(bulk=800.0, rho=25.0, n=400, spe=3, seed=5))
+    write(root + "default/uct.config", "RESOLUTION: 1.0\nVOXEL_DIVISION: 0\n")
+    write(root + "default/cpmg.config", "METHOD: image-based\nOBS_TIME: 12.0\nAPPLY_BULK: true\nSAVE_MODE: true\n"
+                                        "SAVE_DECAY: true\nSAVE_HISTOGRAM: true\nSAVE_WALKERS: true\n")
+    rc = host.cli(["--config-root", root, "--synthetic", IMG_A, "--quiet", "cpmg"], cwd=str(tmp_path))
+    assert rc == 0
+    d = str(tmp_path / "db" / "t") + "//NMR_cpmg_t=12.00ms"
+    decay = np.loadtxt(d + "/cpmg_decay.csv", delimiter=",", skiprows=1)
+    assert np.array_equal(decay[:, 0], golden["cpmg_times"])
+    np.testing.assert_allclose(decay[:, 3], golden["cpmg_signal"], rtol=1e-12)
+    np.testing.assert_allclose(decay[:, 1], golden["cpmg_signal"], rtol=1e-12)
+    coll = np.loadtxt(d + "/cpmg_echo_collisions.csv", delimiter=",", skiprows=1)
+    assert coll.shape == (len(golden["cpmg_times"]) - 1, 2)
+    hist = np.loadtxt(d + "/cpmg_histogram.csv", delimiter=",", skiprows=1)
+    assert hist.shape == (1024, 2) and abs(hist[:, 1].sum() - 1.0) < 1e-12
+    walkers = np.loadtxt(d + "/cpmg_walkers.csv", delimiter=",", skiprows=1)
+    assert np.array_equal(walkers[:, 6].astype(np.int64), golden["cpmg_map_collisions"].astype(np.int64))
+    assert os.path.exists(str(tmp_path / "db" / "t" / "SimInfo.txt"))
+
+
+def test_cli_pfgse_matches_reference_sequence(tmp_path, golden):
+    root = str(tmp_path / "config") + "/"
+    write(root + "default/rwnmr.config", RW.format(bulk=2800.0, rho=5.0, n=500, spe=1, seed=9))
+    write(root + "default/uct.config", "RESOLUTION: 1.0\nVOXEL_DIVISION: 0\n")
+    write(root + "default/pfgse.config",
+          "APPLY_BULK: false\nPULSE_WIDTH: 0.5\nMAX_GRADIENT: {0.0, 0.0, 400.0}\nGRADIENT_SAMPLES: 8\n"
+          "TIME_SEQ: manual\nTIME_SAMPLES: 3\nTIME_VALUES: {0.4, 1.0, 2.5}\nAPPLY_SCALE_FACTOR: false\n"
+          "THRESHOLD_TYPE: samples\nTHRESHOLD_VALUE: 8\nALLOW_WALKER_SAMPLING: false\nSAVE_MODE: true\n"
+          "SAVE_PFGSE: true\n")
+    rc = host.cli(["--config-root", root, "--synthetic", IMG_A, "--quiet", "pfgse"], cwd=str(tmp_path))
+    assert rc == 0
+    d = str(tmp_path / "db" / "t") + "//NMR_pfgse"
+    res = np.loadtxt(d + "/PFGSE_results.csv", delimiter=",", skiprows=1, ndmin=2)
+    np.testing.assert_allclose(res[:, 0], golden["pfgse_delta"], rtol=0)
+    np.testing.assert_allclose(res[:, 1], golden["pfgse_dsat"], rtol=1e-10)
+    np.testing.assert_allclose(res[:, 5], golden["pfgse_dmsd"], rtol=1e-12)
+    for i in range(3):
+        e = np.loadtxt(d + f"/timesamples/echoes_{i}.csv", delimiter=",", skiprows=1)
+        att = e[:, 2] / e[0, 2]
+        assert np.all(np.abs(att - golden["pfgse_Mkt"][i]) <= 1e-12)
+    g = np.loadtxt(d + "/PFGSE_gradient.csv", delimiter=",", skiprows=1)
+    np.testing.assert_allclose(g[:, 4:7], golden["pfgse_kvec"], rtol=1e-15, atol=0)
+
+
+def test_cli_reads_png_stack(tmp_path, golden):
+    """uct-config PNG slices -> same walk as the label volume they encode."""
+    import struct
+    import zlib
+
+    lab = golden["img_a"]
+    nz, ny, nx = lab.shape
+    img_dir = tmp_path / "imgs"
+    img_dir.mkdir()
+    for z in range(nz):
+        raw = b"".join(b"\x00" + bytes((lab[z, y] * 255).astype(np.uint8)) for y in range(ny))
+
+        def chunk(t, dat):
+            return struct.pack(">I", len(dat)) + t + dat + struct.pack(">I", zlib.crc32(t + dat) & 0xFFFFFFFF)
+
+        png = (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", nx, ny, 8, 0, 0, 0, 0)) +
+               chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
+        (img_dir / f"slice_{z:03d}.png").write_bytes(png)
+    root = str(tmp_path / "config") + "/"
+    write(root + "default/rwnmr.config", RW.format(bulk=800.0, rho=25.0, n=400, spe=3, seed=5))
+    write(root + "default/uct.config", f"DIR_PATH: {img_dir}/\nFILENAME: slice_\nFIRST_IDX: 0\nDIGITS: 3\n"
+                                       f"EXTENSION: .png\nSLICES: {nz}\nRESOLUTION: 1.0\nVOXEL_DIVISION: 0\n")
+    write(root + "default/cpmg.config", "OBS_TIME: 12.0\nAPPLY_BULK: true\nSAVE_HISTOGRAM: false\n")
+    assert host.cli(["--config-root", root, "--quiet", "cpmg"], cwd=str(tmp_path)) == 0
+    decay = np.loadtxt(str(tmp_path / "db" / "t") + "//NMR_cpmg_t=12.00ms/cpmg_decay.csv", delimiter=",",
+                       skiprows=1)
+    np.testing.assert_allclose(decay[:, 3], golden["cpmg_signal"], rtol=1e-12)
