@@ -149,6 +149,43 @@ typedef struct rwnmr_noalloc_cpmg_args
 rwnmr_status rwnmr_cpmg_run_noalloc(const rwnmr_cpmg_params *p, const rwnmr_noalloc_cpmg_args *args, char *err,
                                     int errlen);
 
+/* ---- batched multi-image CPMG with a relaxivity population per image ------------------ */
+/* Extends the reference (one image per process, one relaxivity per run): many images of uneven
+ * size and walker count are walked by one persistent work-queue launch, and each image carries up
+ * to 16 candidate decrease factors that one walk evaluates together (trajectories do not depend on
+ * the relaxivity). Per image and candidate the walk returns the normalisation-free echo sums
+ * M_r(e) = sum_w f_r^c_w(e) and, if asked, their exact derivatives dM_r(e)/df_r =
+ * sum_w c_w f_r^(c_w - 1), from which any loss gradient (the adjoint for that candidate) follows on
+ * the host. Single-phase images (labels != 0 are solid). */
+typedef struct rwnmr_batch rwnmr_batch;
+
+typedef struct rwnmr_batch_cpmg_params
+{
+    int32_t bc;                /* RWNMR_BC_* for every image */
+    int32_t steps_per_echo;
+    int32_t n_echoes;
+    int32_t n_candidates;      /* 1..16 decrease factors per image */
+    int32_t derivatives;       /* also return dM/df per candidate */
+    int32_t threads_per_block; /* 0 = autotuned value (or 256 before rwnmr_batch_autotune) */
+    int32_t use_graph;         /* replay the launch sequence as a captured CUDA graph */
+} rwnmr_batch_cpmg_params;
+
+rwnmr_status rwnmr_batch_create(rwnmr_batch **out, int device);
+void rwnmr_batch_destroy(rwnmr_batch *batch);
+const char *rwnmr_batch_last_error(const rwnmr_batch *batch);
+double rwnmr_batch_last_kernel_ms(const rwnmr_batch *batch);
+int64_t rwnmr_batch_launch_count(const rwnmr_batch *batch);
+/* Adds one image (bit-blocks as for rwnmr_image_upload) with its walkers; *index = image number. */
+rwnmr_status rwnmr_batch_add_image(rwnmr_batch *batch, const uint64_t *blocks, int32_t nx, int32_t ny, int32_t nz,
+                                   int64_t n, const int32_t *x0, const int32_t *y0, const int32_t *z0,
+                                   const uint64_t *seed0, int32_t *index);
+/* dfactor [n_images][n_candidates]; echo and decho (nullable) [n_images][n_candidates][n_echoes+1]. */
+rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *batch, const rwnmr_batch_cpmg_params *p, const double *dfactor,
+                              double *echo, double *decho);
+/* Times the walk for 128, 256 and 512 threads per block and keeps the fastest for later calls. */
+rwnmr_status rwnmr_batch_autotune(rwnmr_batch *batch, const rwnmr_batch_cpmg_params *p, int32_t *best_threads,
+                                  double *best_ms);
+
 /* ---- collision-mapping walk ------------------------------------------------------------ */
 /* NMR_Simulation::mapSimulation (NMR_Simulation.cpp:1787-1841; NMR_Simulation_cuda.cpp:726-1270):
  * walks every walker from its initial state for `steps` steps and writes its collision count. */

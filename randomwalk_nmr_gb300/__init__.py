@@ -7,6 +7,6 @@ Layers:
   * ``sim``         Python mirror of the reference's NMR_Simulation / NMR_cpmg / NMR_PFGSE API
   * ``autograd``    torch.autograd.Function wrappers (forward walk + seed-replay adjoint)
 """
-from .engine import Engine, RwnmrError, fx_to_float, load_library, library_path  # noqa: F401
+from .engine import Batch, Engine, RwnmrError, fx_to_float, load_library, library_path  # noqa: F401
 
-__all__ = ["Engine", "RwnmrError", "fx_to_float", "load_library", "library_path"]
+__all__ = ["Batch", "Engine", "RwnmrError", "fx_to_float", "load_library", "library_path"]

@@ -1,0 +1,611 @@
+// Batched multi-image CPMG with a relaxivity population per image (include/rwnmr_gb300.h,
+// rwnmr_batch_*).
+//
+// One persistent kernel walks every image of the batch: CTAs take work items -- up to one CTA's
+// worth of walkers of one image -- from a global queue (largest images first) until it is empty,
+// so uneven images and walker counts share one launch without tail waste. Walk trajectories do
+// not depend on the relaxivity, so each walker's walk serves all candidates of its image at once:
+// after every echo the walker looks up, for each of 16 candidate decrease factors f_r, its energy
+// f_r^c and its derivative c f_r^(c-1) (64-bit fixed-point tables, exact integer sums), and the warp
+// reduces the 16 candidate values together with a recursive-halving shuffle transpose (16 values
+// per lane -> one candidate sum per lane pair in 15 exchanges instead of 16 separate reductions).
+// The echo trains M_r(e) and their derivatives dM_r(e)/df_r come out of one walk, so both the
+// forward model and its vector-Jacobian product (the adjoint for one parameter per candidate) of
+// all 16 candidates of all images cost one launch.
+//
+// The sequence table kernel -> accumulator reset -> walk -> copy-out is captured once in a CUDA
+// graph and replayed for every new set of candidates (a fit iteration changes only the pinned
+// decrease-factor buffer). The block size is chosen by a short timed sweep (rwnmr_batch_autotune).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/rwnmr_gb300.h"
+#include "walk_device.cuh"
+#include "walk_kernels.cuh"
+
+using namespace rwnmr;
+
+namespace
+{
+constexpr int kCand = 16;             // candidate slots per image
+constexpr int kWin = 16;              // echoes per shared-memory window
+constexpr double kEScale = 288230376151711744.0; // 2^58: energy scale (32 lanes sum below 2^63)
+constexpr unsigned FULLM = 0xffffffffu;
+
+struct BatchImage
+{
+    const uint64_t *blocks;
+    int32_t nx, ny, nz, bcols, bcr;
+    int64_t walker0, n;       // walker range in the batch arrays
+    int64_t acc0;             // offset of this image's accumulators (u64 words)
+    int64_t tab0;             // offset of this image's tables (u64 words)
+    int32_t u_shift;          // derivative scale exponent
+};
+
+struct WorkItem
+{
+    int32_t image;
+    int32_t pad;
+    int64_t first, last; // walker range [first, last)
+};
+
+struct BatchLaunch
+{
+    const BatchImage *images;
+    const WorkItem *items;
+    int32_t n_items;
+    int32_t n_echoes, steps_per_echo, bc;
+    int32_t deriv;
+    int32_t tstride;             // entries per candidate table (n_echoes * steps_per_echo + 1)
+    const unsigned long long *tab; // [image][cand][2][tstride]: energy, derivative
+    unsigned long long *acc;       // [image][n_echoes + 1][cand][4]: energy lo/hi, derivative lo/hi
+    const int32_t *x0, *y0, *z0;
+    const uint64_t *seed0;
+    unsigned *counter;
+    unsigned *status;
+};
+
+// Sum over the warp of v[0..15] per candidate: after the exchanges lane l holds candidate l >> 1's
+// warp total (lanes 2c and 2c+1 hold the same value).
+__device__ __forceinline__ unsigned long long transpose_reduce16(unsigned long long (&v)[kCand], int lane)
+{
+#pragma unroll
+    for (int half = 8; half >= 1; half >>= 1)
+    {
+        const int mask = half * 2; // xor distance 16, 8, 4, 2
+        const bool upper = (lane & mask) != 0;
+#pragma unroll
+        for (int k = 0; k < half; k++)
+        {
+            // keep the half of the vector this lane is responsible for, send the other half
+            const unsigned long long send = upper ? v[k] : v[k + half];
+            const unsigned long long keep = upper ? v[k + half] : v[k];
+            const unsigned long long got = __shfl_xor_sync(FULLM, send, mask);
+            v[k] = keep + got;
+        }
+    }
+    return v[0] + __shfl_xor_sync(FULLM, v[0], 1);
+}
+
+template <int BC>
+__global__ void __launch_bounds__(512) batch_cpmg_kernel(BatchLaunch L)
+{
+    extern __shared__ unsigned long long sacc[]; // [kWin][kCand][4]
+    __shared__ int s_item;
+    const int lane = threadIdx.x & 31;
+    for (;;)
+    {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(L.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= L.n_items) break;
+        const WorkItem w = L.items[item];
+        const BatchImage img = L.images[w.image];
+        DevImage im;
+        im.blocks = img.blocks;
+        im.nx = img.nx;
+        im.ny = img.ny;
+        im.nz = img.nz;
+        im.bcols = img.bcols;
+        im.bcr = img.bcr;
+        im.bc = L.bc;
+        im.shift = 0;
+        const int64_t i = w.first + threadIdx.x;
+        bool active = i < w.last;
+        WalkerPos p{};
+        uint64_t seed = 0;
+        if (active)
+        {
+            p.x = L.x0[i];
+            p.y = L.y0[i];
+            p.z = L.z0[i];
+            seed = L.seed0[i];
+            if (!start_ok<BC>(im, p))
+            {
+                atomicOr(L.status, kStatusBadStart);
+                active = false;
+            }
+            init_image_coords<BC>(im, p);
+        }
+        const unsigned long long *tabE = L.tab + img.tab0;
+        unsigned long long *acc = L.acc + img.acc0;
+        uint32_t c = 0;
+        for (int k = threadIdx.x; k < kWin * kCand * 4; k += blockDim.x) sacc[k] = 0;
+        __syncthreads();
+        for (int e0 = -1; e0 < L.n_echoes; e0 += kWin)
+        {
+            // window covers output echoes [e0 + 1, e1]; output 0 (initial state) comes first
+            const int e1 = min(e0 + kWin, L.n_echoes);
+            for (int e = e0 + 1; e <= e1; e++)
+            {
+                if (active && e > 0)
+                    for (int s = 0; s < L.steps_per_echo; s++)
+                    {
+                        bool wall;
+                        int ph;
+                        walker_step<BC, 1>(im, p, seed, wall, ph);
+                        c += wall ? 1u : 0u;
+                    }
+                unsigned long long v[kCand];
+#pragma unroll
+                for (int r = 0; r < kCand; r++)
+                    v[r] = active ? __ldg(tabE + ((size_t)r * 2) * L.tstride + c) : 0ull;
+                const unsigned long long sumE = transpose_reduce16(v, lane);
+                const int slot = e - (e0 + 1);
+                // a warp sum is below 2^63; its 32-bit halves accumulate without overflow
+                unsigned long long *sa = &sacc[(slot * kCand + (lane >> 1)) * 4];
+                if ((lane & 1) == 0)
+                {
+                    atomicAdd(&sa[0], sumE & 0xffffffffull);
+                    atomicAdd(&sa[1], sumE >> 32);
+                }
+                if (L.deriv)
+                {
+#pragma unroll
+                    for (int r = 0; r < kCand; r++)
+                        v[r] = active ? __ldg(tabE + ((size_t)r * 2 + 1) * L.tstride + c) : 0ull;
+                    const unsigned long long sumU = transpose_reduce16(v, lane);
+                    if ((lane & 1) == 0)
+                    {
+                        atomicAdd(&sa[2], sumU & 0xffffffffull);
+                        atomicAdd(&sa[3], sumU >> 32);
+                    }
+                }
+            }
+            __syncthreads();
+            const int nslots = e1 - e0;
+            for (int k = threadIdx.x; k < nslots * kCand * 4; k += blockDim.x)
+            {
+                const unsigned long long val = sacc[k];
+                if (val) atomicAdd(&acc[(size_t)(e0 + 1) * kCand * 4 + k], val);
+                sacc[k] = 0;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Tables for every (image, candidate): energy round(f^c 2^58) and derivative round(c f^(c-1) 2^us),
+// f^c the FP64 repeated product. One thread per (image, candidate).
+__global__ void batch_tables_kernel(const double *__restrict__ f, int n_images, const int32_t *__restrict__ ushift,
+                                    int tstride, unsigned long long *__restrict__ tab)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_images * kCand) return;
+    const int img = t / kCand;
+    const double fr = f[t];
+    const double us = ldexp(1.0, ushift[img]);
+    unsigned long long *te = tab + ((size_t)t * 2) * tstride;
+    unsigned long long *tu = te + tstride;
+    double v = 1.0, prev = 0.0;
+    for (int k = 0; k < tstride; k++)
+    {
+        te[k] = __double2ull_rn(v * kEScale);
+        tu[k] = k == 0 ? 0ull : __double2ull_rn((double)k * prev * us);
+        prev = v;
+        v = v * fr;
+    }
+}
+
+rwnmr_status put(std::string &s, rwnmr_status st, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    s = buf;
+    return st;
+}
+} // namespace
+
+struct rwnmr_batch
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // host copies of the inputs until the first run uploads them
+    std::vector<BatchImage> images;
+    std::vector<std::vector<uint64_t>> h_blocks;
+    std::vector<int32_t> hx, hy, hz;
+    std::vector<uint64_t> hs;
+    bool uploaded = false;
+    // device
+    uint64_t *d_blocks = nullptr;
+    BatchImage *d_images = nullptr;
+    WorkItem *d_items = nullptr;
+    int32_t *d_x = nullptr, *d_y = nullptr, *d_z = nullptr, *d_ushift = nullptr;
+    uint64_t *d_seed = nullptr;
+    unsigned long long *d_tab = nullptr, *d_acc = nullptr;
+    unsigned *d_counter = nullptr, *d_status = nullptr;
+    double *d_f = nullptr;
+    size_t tab_words = 0, acc_words = 0;
+    int n_items = 0, items_block = 0;
+    // pinned host staging and the captured graph
+    double *h_f = nullptr;
+    unsigned long long *h_acc = nullptr;
+    unsigned *h_status = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_key[5] = {0, 0, 0, 0, 0};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
+    int64_t launches = 0;
+    int tuned_block = 0;
+    int sms = 0;
+
+    void free_device()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        for (void *p : {(void *)d_blocks, (void *)d_images, (void *)d_items, (void *)d_x, (void *)d_y, (void *)d_z,
+                        (void *)d_ushift, (void *)d_seed, (void *)d_tab, (void *)d_acc, (void *)d_counter,
+                        (void *)d_status, (void *)d_f})
+            if (p) cudaFree(p);
+        d_blocks = nullptr;
+        d_images = nullptr;
+        d_items = nullptr;
+        d_x = d_y = d_z = d_ushift = nullptr;
+        d_seed = nullptr;
+        d_tab = d_acc = nullptr;
+        d_counter = d_status = nullptr;
+        d_f = nullptr;
+        if (h_f) cudaFreeHost(h_f);
+        if (h_acc) cudaFreeHost(h_acc);
+        if (h_status) cudaFreeHost(h_status);
+        h_f = nullptr;
+        h_acc = nullptr;
+        h_status = nullptr;
+        uploaded = false;
+    }
+};
+
+namespace
+{
+#define BT_CUDA(b, expr, what)                                                                                         \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        cudaError_t _e = (expr);                                                                                       \
+        if (_e != cudaSuccess)                                                                                         \
+            return put((b)->err, _e == cudaErrorMemoryAllocation ? RWNMR_ERR_NOMEM : RWNMR_ERR_CUDA, "%s: %s", what,  \
+                       cudaGetErrorString(_e));                                                                        \
+    } while (0)
+
+rwnmr_status upload(rwnmr_batch *b, int n_echoes, int spe)
+{
+    const int64_t nmax = (int64_t)n_echoes * spe;
+    const int tstride = (int)(nmax + 1);
+    const int ni = (int)b->images.size();
+    if (b->uploaded && b->tab_words == (size_t)ni * kCand * 2 * tstride &&
+        b->acc_words == (size_t)ni * (n_echoes + 1) * kCand * 4)
+        return RWNMR_OK;
+    b->free_device();
+    size_t nb = 0;
+    for (auto &h : b->h_blocks) nb += h.size();
+    const size_t nw = b->hx.size();
+    BT_CUDA(b, cudaMalloc(&b->d_blocks, std::max<size_t>(nb, 1) * 8), "batch image");
+    BT_CUDA(b, cudaMalloc(&b->d_x, std::max<size_t>(nw, 1) * 4), "batch walkers");
+    BT_CUDA(b, cudaMalloc(&b->d_y, std::max<size_t>(nw, 1) * 4), "batch walkers");
+    BT_CUDA(b, cudaMalloc(&b->d_z, std::max<size_t>(nw, 1) * 4), "batch walkers");
+    BT_CUDA(b, cudaMalloc(&b->d_seed, std::max<size_t>(nw, 1) * 8), "batch walkers");
+    size_t off = 0;
+    std::vector<int32_t> ushift(ni);
+    const int us = 58 - (int)std::ceil(std::log2((double)(nmax + 2)));
+    for (int k = 0; k < ni; k++)
+    {
+        BT_CUDA(b, cudaMemcpy(b->d_blocks + off, b->h_blocks[k].data(), b->h_blocks[k].size() * 8, cudaMemcpyHostToDevice),
+                "batch image upload");
+        b->images[k].blocks = b->d_blocks + off;
+        off += b->h_blocks[k].size();
+        b->images[k].tab0 = (int64_t)k * kCand * 2 * tstride;
+        b->images[k].acc0 = (int64_t)k * (n_echoes + 1) * kCand * 4;
+        b->images[k].u_shift = us;
+        ushift[k] = us;
+    }
+    if (nw)
+    {
+        BT_CUDA(b, cudaMemcpy(b->d_x, b->hx.data(), nw * 4, cudaMemcpyHostToDevice), "batch walkers upload");
+        BT_CUDA(b, cudaMemcpy(b->d_y, b->hy.data(), nw * 4, cudaMemcpyHostToDevice), "batch walkers upload");
+        BT_CUDA(b, cudaMemcpy(b->d_z, b->hz.data(), nw * 4, cudaMemcpyHostToDevice), "batch walkers upload");
+        BT_CUDA(b, cudaMemcpy(b->d_seed, b->hs.data(), nw * 8, cudaMemcpyHostToDevice), "batch walkers upload");
+    }
+    BT_CUDA(b, cudaMalloc(&b->d_images, std::max(ni, 1) * sizeof(BatchImage)), "batch descriptors");
+    BT_CUDA(b, cudaMemcpy(b->d_images, b->images.data(), ni * sizeof(BatchImage), cudaMemcpyHostToDevice), "batch descriptors");
+    BT_CUDA(b, cudaMalloc(&b->d_ushift, std::max(ni, 1) * 4), "batch descriptors");
+    BT_CUDA(b, cudaMemcpy(b->d_ushift, ushift.data(), ni * 4, cudaMemcpyHostToDevice), "batch descriptors");
+    b->tab_words = (size_t)ni * kCand * 2 * tstride;
+    b->acc_words = (size_t)ni * (n_echoes + 1) * kCand * 4;
+    BT_CUDA(b, cudaMalloc(&b->d_tab, std::max<size_t>(b->tab_words, 1) * 8), "batch tables");
+    BT_CUDA(b, cudaMalloc(&b->d_acc, std::max<size_t>(b->acc_words, 1) * 8), "batch accumulators");
+    BT_CUDA(b, cudaMalloc(&b->d_counter, 4), "batch counter");
+    BT_CUDA(b, cudaMalloc(&b->d_status, 4), "batch status");
+    BT_CUDA(b, cudaMalloc(&b->d_f, std::max(ni, 1) * kCand * 8), "batch factors");
+    BT_CUDA(b, cudaMallocHost(&b->h_f, std::max(ni, 1) * kCand * 8), "batch staging");
+    BT_CUDA(b, cudaMallocHost(&b->h_acc, std::max<size_t>(b->acc_words, 1) * 8), "batch staging");
+    BT_CUDA(b, cudaMallocHost(&b->h_status, 4), "batch staging");
+    b->items_block = 0;
+    b->uploaded = true;
+    return RWNMR_OK;
+}
+
+// Work items of `block` walkers, largest images first.
+rwnmr_status build_items(rwnmr_batch *b, int block)
+{
+    if (b->items_block == block && b->d_items) return RWNMR_OK;
+    std::vector<int> order(b->images.size());
+    for (size_t k = 0; k < order.size(); k++) order[k] = (int)k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->images[a].n > b->images[c].n; });
+    std::vector<WorkItem> items;
+    for (int k : order)
+        for (int64_t s = 0; s < b->images[k].n; s += block)
+            items.push_back({k, 0, b->images[k].walker0 + s, b->images[k].walker0 + std::min<int64_t>(b->images[k].n, s + block)});
+    if (b->d_items) cudaFree(b->d_items);
+    b->d_items = nullptr;
+    BT_CUDA(b, cudaMalloc(&b->d_items, std::max<size_t>(items.size(), 1) * sizeof(WorkItem)), "work items");
+    if (!items.empty())
+        BT_CUDA(b, cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "work items");
+    b->n_items = (int)items.size();
+    b->items_block = block;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    return RWNMR_OK;
+}
+
+cudaError_t enqueue(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block)
+{
+    const int ni = (int)b->images.size();
+    const int tstride = p->n_echoes * p->steps_per_echo + 1;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(b->d_f, b->h_f, (size_t)ni * kCand * 8, cudaMemcpyHostToDevice, b->stream))) return e;
+    batch_tables_kernel<<<(ni * kCand + 127) / 128, 128, 0, b->stream>>>(b->d_f, ni, b->d_ushift, tstride, b->d_tab);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = cudaMemsetAsync(b->d_acc, 0, b->acc_words * 8, b->stream))) return e;
+    if ((e = cudaMemsetAsync(b->d_counter, 0, 4, b->stream))) return e;
+    if ((e = cudaMemsetAsync(b->d_status, 0, 4, b->stream))) return e;
+    BatchLaunch L{};
+    L.images = b->d_images;
+    L.items = b->d_items;
+    L.n_items = b->n_items;
+    L.n_echoes = p->n_echoes;
+    L.steps_per_echo = p->steps_per_echo;
+    L.bc = p->bc;
+    L.deriv = p->derivatives ? 1 : 0;
+    L.tstride = tstride;
+    L.tab = b->d_tab;
+    L.acc = b->d_acc;
+    L.x0 = b->d_x;
+    L.y0 = b->d_y;
+    L.z0 = b->d_z;
+    L.seed0 = b->d_seed;
+    L.counter = b->d_counter;
+    L.status = b->d_status;
+    const size_t smem = (size_t)kWin * kCand * 4 * 8;
+    int per_sm = 1;
+    auto occ = [&](auto kern) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
+        const int grid = std::max(1, std::min(b->n_items, std::max(1, per_sm) * b->sms));
+        kern<<<grid, block, smem, b->stream>>>(L);
+    };
+    if (p->bc == RWNMR_BC_PERIODIC) occ(batch_cpmg_kernel<BC_PERIODIC>);
+    else if (p->bc == RWNMR_BC_MIRROR) occ(batch_cpmg_kernel<BC_MIRROR>);
+    else occ(batch_cpmg_kernel<BC_NOFLUX>);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = cudaMemcpyAsync(b->h_acc, b->d_acc, b->acc_words * 8, cudaMemcpyDeviceToHost, b->stream))) return e;
+    return cudaMemcpyAsync(b->h_status, b->d_status, 4, cudaMemcpyDeviceToHost, b->stream);
+}
+
+rwnmr_status check_params(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
+{
+    if (!p) return put(b->err, RWNMR_ERR_INVALID, "params is NULL");
+    if (b->images.empty()) return put(b->err, RWNMR_ERR_STATE, "batch has no images");
+    if (p->bc < RWNMR_BC_NOFLUX || p->bc > RWNMR_BC_MIRROR) return put(b->err, RWNMR_ERR_INVALID, "unknown boundary condition");
+    if (p->n_echoes < 0 || p->steps_per_echo < 1) return put(b->err, RWNMR_ERR_INVALID, "bad echo count / steps per echo");
+    if (p->n_candidates < 1 || p->n_candidates > kCand)
+        return put(b->err, RWNMR_ERR_INVALID, "1 to %d relaxivity candidates per image", kCand);
+    if ((int64_t)p->n_echoes * p->steps_per_echo > (1 << 24)) return put(b->err, RWNMR_ERR_UNSUPPORTED, "walk too long for the batch tables");
+    if (p->threads_per_block != 0 && (p->threads_per_block % 32 || p->threads_per_block < 64 || p->threads_per_block > 512))
+        return put(b->err, RWNMR_ERR_INVALID, "threads_per_block must be a multiple of 32 in 64..512");
+    return RWNMR_OK;
+}
+} // namespace
+
+extern "C" {
+
+rwnmr_status rwnmr_batch_create(rwnmr_batch **out, int device)
+{
+    if (!out) return RWNMR_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) return RWNMR_ERR_CUDA;
+    if (device < 0 || device >= count) return RWNMR_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return RWNMR_ERR_CUDA;
+    rwnmr_batch *b = new rwnmr_batch();
+    b->device = device;
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
+    {
+        rwnmr_batch_destroy(b);
+        return RWNMR_ERR_CUDA;
+    }
+    *out = b;
+    return RWNMR_OK;
+}
+
+void rwnmr_batch_destroy(rwnmr_batch *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    b->free_device();
+    if (b->d_items) cudaFree(b->d_items);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+const char *rwnmr_batch_last_error(const rwnmr_batch *b) { return b ? b->err.c_str() : "null batch"; }
+double rwnmr_batch_last_kernel_ms(const rwnmr_batch *b) { return b ? b->last_ms : 0.0; }
+int64_t rwnmr_batch_launch_count(const rwnmr_batch *b) { return b ? b->launches : 0; }
+
+rwnmr_status rwnmr_batch_add_image(rwnmr_batch *b, const uint64_t *blocks, int32_t nx, int32_t ny, int32_t nz,
+                                   int64_t n, const int32_t *x0, const int32_t *y0, const int32_t *z0,
+                                   const uint64_t *seed0, int32_t *index)
+{
+    if (!b) return RWNMR_ERR_INVALID;
+    if (!blocks || nx < 2 || ny < 2 || nz < 2) return put(b->err, RWNMR_ERR_INVALID, "bad image");
+    if (n < 0 || (n > 0 && (!x0 || !y0 || !z0 || !seed0))) return put(b->err, RWNMR_ERR_INVALID, "bad walkers");
+    // walkers must start inside the image (checked here so that the kernel's status word only
+    // ever reports engine faults)
+    for (int64_t i = 0; i < n; i++)
+        if ((unsigned)x0[i] >= (unsigned)nx || (unsigned)y0[i] >= (unsigned)ny || (unsigned)z0[i] >= (unsigned)nz)
+            return put(b->err, RWNMR_ERR_INVALID, "walker %lld starts outside the image", (long long)i);
+    BatchImage im{};
+    im.nx = nx;
+    im.ny = ny;
+    im.nz = nz;
+    im.bcols = (nx + 3) / 4;
+    im.bcr = im.bcols * ((ny + 3) / 4);
+    im.walker0 = (int64_t)b->hx.size();
+    im.n = n;
+    const size_t nb = (size_t)im.bcr * ((nz + 3) / 4);
+    b->h_blocks.emplace_back(blocks, blocks + nb);
+    b->hx.insert(b->hx.end(), x0, x0 + n);
+    b->hy.insert(b->hy.end(), y0, y0 + n);
+    b->hz.insert(b->hz.end(), z0, z0 + n);
+    b->hs.insert(b->hs.end(), seed0, seed0 + n);
+    b->images.push_back(im);
+    b->free_device();
+    if (b->d_items) cudaFree(b->d_items);
+    b->d_items = nullptr;
+    b->items_block = 0;
+    if (index) *index = (int32_t)b->images.size() - 1;
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, const double *dfactor, double *echo,
+                              double *decho)
+{
+    if (!b) return RWNMR_ERR_INVALID;
+    rwnmr_status st = check_params(b, p);
+    if (st != RWNMR_OK) return st;
+    if (!dfactor) return put(b->err, RWNMR_ERR_INVALID, "dfactor is NULL");
+    const int ni = (int)b->images.size();
+    const int R = p->n_candidates;
+    for (int k = 0; k < ni * R; k++)
+        if (!(dfactor[k] >= 0.0 && dfactor[k] <= 1.0))
+            return put(b->err, RWNMR_ERR_UNSUPPORTED, "decrease factor %g outside [0, 1]", dfactor[k]);
+    cudaSetDevice(b->device);
+    if ((st = upload(b, p->n_echoes, p->steps_per_echo)) != RWNMR_OK) return st;
+    const int block = p->threads_per_block ? p->threads_per_block : (b->tuned_block ? b->tuned_block : 256);
+    if ((st = build_items(b, block)) != RWNMR_OK) return st;
+    for (int k = 0; k < ni; k++)
+        for (int r = 0; r < kCand; r++) b->h_f[k * kCand + r] = r < R ? dfactor[k * R + r] : 1.0;
+    const int key[5] = {p->n_echoes, p->steps_per_echo, p->bc, p->derivatives ? 1 : 0, block};
+    BT_CUDA(b, cudaEventRecord(b->ev0, b->stream), "event");
+    if (p->use_graph)
+    {
+        if (!b->graph || std::memcmp(key, b->graph_key, sizeof key) != 0)
+        {
+            if (b->graph) cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+            cudaGraph_t g;
+            BT_CUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+            cudaError_t ce = enqueue(b, p, block);
+            cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
+            BT_CUDA(b, ce, "graph capture");
+            BT_CUDA(b, ee, "graph capture");
+            ce = cudaGraphInstantiate(&b->graph, g, 0);
+            cudaGraphDestroy(g);
+            BT_CUDA(b, ce, "graph instantiate");
+            std::memcpy(b->graph_key, key, sizeof key);
+        }
+        BT_CUDA(b, cudaGraphLaunch(b->graph, b->stream), "graph launch");
+    }
+    else
+        BT_CUDA(b, enqueue(b, p, block), "batch launch");
+    b->launches += 2;
+    BT_CUDA(b, cudaEventRecord(b->ev1, b->stream), "event");
+    BT_CUDA(b, cudaStreamSynchronize(b->stream), "batch walk");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    b->last_ms = ms;
+    if (*b->h_status & kStatusBadStart) return put(b->err, RWNMR_ERR_INVALID, "a walker starts outside its image");
+    const int E1 = p->n_echoes + 1;
+    for (int k = 0; k < ni; k++)
+    {
+        const double ds = std::ldexp(1.0, -b->images[k].u_shift);
+        const unsigned long long *a = b->h_acc + b->images[k].acc0;
+        for (int r = 0; r < R; r++)
+            for (int e = 0; e < E1; e++)
+            {
+                const unsigned long long *v = a + ((size_t)e * kCand + r) * 4;
+                const size_t o = ((size_t)k * R + r) * E1 + e;
+                const unsigned __int128 se = (unsigned __int128)v[0] + ((unsigned __int128)v[1] << 32);
+                const unsigned __int128 su = (unsigned __int128)v[2] + ((unsigned __int128)v[3] << 32);
+                if (echo) echo[o] = (double)se / kEScale;
+                if (decho) decho[o] = p->derivatives ? (double)su * ds : 0.0;
+            }
+    }
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_batch_autotune(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int32_t *best_threads,
+                                  double *best_ms)
+{
+    if (!b) return RWNMR_ERR_INVALID;
+    rwnmr_status st = check_params(b, p);
+    if (st != RWNMR_OK) return st;
+    const int ni = (int)b->images.size();
+    std::vector<double> f((size_t)ni * p->n_candidates, 0.999);
+    double best = 1e30;
+    int arg = 256;
+    for (int t : {128, 256, 512})
+    {
+        rwnmr_batch_cpmg_params q = *p;
+        q.threads_per_block = t;
+        q.use_graph = 0;
+        if ((st = rwnmr_batch_cpmg(b, &q, f.data(), nullptr, nullptr)) != RWNMR_OK) return st;
+        if ((st = rwnmr_batch_cpmg(b, &q, f.data(), nullptr, nullptr)) != RWNMR_OK) return st;
+        if (b->last_ms < best)
+        {
+            best = b->last_ms;
+            arg = t;
+        }
+    }
+    b->tuned_block = arg;
+    if (best_threads) *best_threads = arg;
+    if (best_ms) *best_ms = best;
+    return RWNMR_OK;
+}
+
+} // extern "C"

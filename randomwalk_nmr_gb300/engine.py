@@ -35,7 +35,9 @@ EXPORTS = [
     "rwnmr_ctx_launch_count", "rwnmr_ctx_last_kernel_ms", "rwnmr_image_upload", "rwnmr_image_upload_labels",
     "rwnmr_image_download_blocks", "rwnmr_walkers_upload", "rwnmr_walkers_download", "rwnmr_cpmg_run",
     "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_map_continue", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
-    "rwnmr_cpmg_run_noalloc",
+    "rwnmr_cpmg_run_noalloc", "rwnmr_batch_create", "rwnmr_batch_destroy", "rwnmr_batch_last_error",
+    "rwnmr_batch_last_kernel_ms", "rwnmr_batch_launch_count", "rwnmr_batch_add_image", "rwnmr_batch_cpmg",
+    "rwnmr_batch_autotune",
 ]
 
 
@@ -86,6 +88,13 @@ def load_library(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.rwnmr_ctx_last_kernel_ms.restype = ctypes.c_double
         lib.rwnmr_ctx_last_kernel_ms.argtypes = [_vp]
         lib.rwnmr_ctx_destroy.argtypes = [_vp]
+        lib.rwnmr_batch_last_error.restype = ctypes.c_char_p
+        lib.rwnmr_batch_last_error.argtypes = [_vp]
+        lib.rwnmr_batch_last_kernel_ms.restype = ctypes.c_double
+        lib.rwnmr_batch_last_kernel_ms.argtypes = [_vp]
+        lib.rwnmr_batch_launch_count.restype = ctypes.c_int64
+        lib.rwnmr_batch_launch_count.argtypes = [_vp]
+        lib.rwnmr_batch_destroy.argtypes = [_vp]
         for name in EXPORTS:
             getattr(lib, name)  # raises AttributeError if a declared symbol is missing
         _LIB = lib
@@ -242,6 +251,81 @@ class Engine:
         out = np.zeros((prm.n_delta, prm.n_g))
         self._check(self.lib.rwnmr_pfgse_grad_g(self.ctx, ctypes.byref(prm), ctypes.c_double(kscale), _p(d), _p(out)))
         return out
+
+
+class BatchParams(ctypes.Structure):
+    _fields_ = [("bc", ctypes.c_int32), ("steps_per_echo", ctypes.c_int32), ("n_echoes", ctypes.c_int32),
+                ("n_candidates", ctypes.c_int32), ("derivatives", ctypes.c_int32),
+                ("threads_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32)]
+
+
+class Batch:
+    """Many images, each with its walkers and up to 16 relaxivity candidates, walked by one
+    persistent launch (rwnmr_batch_*)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        b = _vp()
+        st = self.lib.rwnmr_batch_create(ctypes.byref(b), int(device))
+        if st != 0:
+            raise RwnmrError(st, f"could not create a batch on device {device}")
+        self.b = b
+        self.n_images = 0
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.rwnmr_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != 0:
+            raise RwnmrError(st, self.lib.rwnmr_batch_last_error(self.b).decode())
+
+    def add_image(self, blocks, shape, x0, y0, z0, seed0) -> int:
+        blocks = np.ascontiguousarray(blocks, np.uint64)
+        nz, ny, nx = shape
+        arrs = [np.ascontiguousarray(a, t) for a, t in ((x0, np.int32), (y0, np.int32), (z0, np.int32),
+                                                          (seed0, np.uint64))]
+        idx = ctypes.c_int32()
+        self._check(self.lib.rwnmr_batch_add_image(self.b, _p(blocks), nx, ny, nz, ctypes.c_int64(len(arrs[0])),
+                                                   *[_p(a) for a in arrs], ctypes.byref(idx)))
+        self.n_images += 1
+        return idx.value
+
+    def cpmg(self, dfactor, n_echoes: int, steps_per_echo: int, derivatives: bool = True, bc: str = "noflux",
+             threads_per_block: int = 0, use_graph: bool = True):
+        f = np.ascontiguousarray(dfactor, np.float64)
+        if f.ndim == 1:
+            f = f[:, None]
+        R = f.shape[1]
+        prm = BatchParams(BC[bc], int(steps_per_echo), int(n_echoes), R, int(bool(derivatives)),
+                          int(threads_per_block), int(bool(use_graph)))
+        echo = np.zeros((self.n_images, R, n_echoes + 1))
+        decho = np.zeros_like(echo) if derivatives else None
+        self._check(self.lib.rwnmr_batch_cpmg(self.b, ctypes.byref(prm), _p(f), _p(echo), _p(decho)))
+        return echo, decho
+
+    def autotune(self, n_echoes: int, steps_per_echo: int, n_candidates: int = 16, derivatives: bool = True,
+                 bc: str = "noflux"):
+        prm = BatchParams(BC[bc], int(steps_per_echo), int(n_echoes), int(n_candidates), int(bool(derivatives)), 0, 0)
+        t = ctypes.c_int32()
+        ms = ctypes.c_double()
+        self._check(self.lib.rwnmr_batch_autotune(self.b, ctypes.byref(prm), ctypes.byref(t), ctypes.byref(ms)))
+        return t.value, ms.value
+
+    @property
+    def last_kernel_ms(self) -> float:
+        return float(self.lib.rwnmr_batch_last_kernel_ms(self.b))
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.rwnmr_batch_launch_count(self.b))
 
 
 def fx_to_float(limbs) -> np.ndarray:
