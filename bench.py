@@ -193,6 +193,146 @@ def run_reference(args, w):
     print(json.dumps(line))
 
 
+def _sphere_image(args):
+    from randomwalk_nmr_gb300 import host
+
+    shape, rmin, rmax, por, phases, seed, walkers, wseed = args
+    lab, p = host.synth_spheres(shape, rmin, rmax, por, phases, seed=seed)
+    blocks, _ = host.pack_blocks(lab)
+    w = host.place_walkers(blocks, lab.shape, walkers, wseed)[:4]
+    return lab, blocks, w, p
+
+
+def run_fit_multiphase(args):
+    """Differentiable CPMG fit (BASELINE configs[3]): 200^3, 4 solid phases, 500k walkers, 5000 echoes
+    of 3 steps; L-BFGS with adjoint gradients vs the restated GA (population 64) on the same GPU walk."""
+    import torch
+
+    from randomwalk_nmr_gb300 import Engine
+    from randomwalk_nmr_gb300.autograd import cpmg_decay
+    from randomwalk_nmr_gb300.fit import fit_rho_adjoint
+    from randomwalk_nmr_gb300.ga import GeneticAlgorithm, misfit_fitness
+
+    small = args.workload.endswith("-small")
+    n, echoes, edge = (50_000, 500, 100) if small else (500_000, 5000, 200)
+    lab, blocks, w, por = _sphere_image(((edge, edge, edge), 5.0, 12.0, 0.30, 4, 4, n, 7))
+    eng = Engine(0)
+    eng.upload_labels(lab, 4)
+    eng.upload_walkers(*w)
+    rng = np.random.default_rng(5)
+    hidden = rng.uniform(2.0, 40.0, 4)
+    t2b, spe = 2000.0, 3
+    with torch.no_grad():
+        clean = cpmg_decay(torch.tensor(hidden), torch.tensor(t2b), eng, echoes, spe).numpy()
+    target = clean + rng.normal(0.0, 1e-3, clean.shape)
+    res = fit_rho_adjoint(eng, target, np.full(4, 20.0), echoes, spe, t2b, max_evals=args.fit_evals)
+
+    def model(g):
+        with torch.no_grad():
+            m = cpmg_decay(torch.tensor(np.asarray(g)), torch.tensor(t2b), eng, echoes, spe).numpy()
+        ga_gpu[0] += eng.last_kernel_ms * 1e-3
+        return m
+
+    ga_gpu = [0.0]
+    t0 = time.perf_counter()
+    ga = GeneticAlgorithm(misfit_fitness(model, target, 1e-3), [2.0] * 4, [40.0] * 4, population=64, seed=11)
+    ga.run(args.ga_generations)
+    ga_wall = time.perf_counter() - t0
+    line = {"metric": "GPU-seconds of the relaxivity fit (multi-phase CPMG)", "value": res["gpu_seconds"],
+            "unit": "GPU-s", "higher_is_better": False, "impl": "gb300",
+            "config": {"workload": args.workload, "image": f"{edge}^3, 4 phases, porosity {por:.3f}",
+                       "walkers": n, "echoes": echoes, "steps_per_echo": spe, "T2b_ms": t2b,
+                       "noise_sigma": 1e-3},
+            "gradient_fit": {"gpu_seconds": res["gpu_seconds"], "walks": res["walks"], "evals": res["evals"],
+                             "rho": res["rho"].tolist(), "hidden_rho": hidden.tolist(), "loss": res["loss"],
+                             "wall_seconds": res["wall_seconds"]},
+            "ga_fit": {"gpu_seconds": ga_gpu[0], "walks": ga.evaluations, "generations": args.ga_generations,
+                       "population": 64, "rho": ga.best[0].tolist(), "fitness": ga.best[1], "wall_seconds": ga_wall},
+            "gpu_seconds_ratio_ga_over_gradient": ga_gpu[0] / max(res["gpu_seconds"], 1e-12)}
+    print(json.dumps(line))
+    eng.close()
+
+
+def run_fit_batch(args):
+    """Batched uneven workload (BASELINE configs[4]): 64 sphere packs with edges U[64, 320], walkers
+    U[1e4, 5e5], 16 relaxivity candidates per image, 3000 echoes of 3 steps, one persistent launch per
+    fit iteration (CUDA graph, autotuned block size), vs per-image plain CPMG + the restated GA."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from randomwalk_nmr_gb300 import Batch, Engine
+    from randomwalk_nmr_gb300.autograd import echo_times
+    from randomwalk_nmr_gb300.fit import decrease_factor, fit_rho_batch
+    from randomwalk_nmr_gb300.ga import GeneticAlgorithm, misfit_fitness
+
+    small = args.workload.endswith("-small")
+    n_img = 8 if small else 64
+    echoes, spe, t2b = (300 if small else 3000), 3, 2800.0
+    rng = np.random.default_rng(100)
+    specs = []
+    for k in range(n_img):
+        edge = int(rng.integers(64, 321)) if not small else int(rng.integers(32, 81))
+        nw = int(rng.integers(10_000, 500_001)) if not small else int(rng.integers(2_000, 20_001))
+        specs.append(((edge,) * 3, 3.0, 15.0, float(rng.uniform(0.15, 0.40)), 1, 100 + k, nw, 1000 + k))
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+        imgs = list(ex.map(_sphere_image, specs))
+    setup_s = time.perf_counter() - t0
+    b = Batch(0)
+    for lab, blocks, w, por in imgs:
+        b.add_image(blocks, lab.shape, *w)
+    nwalk = np.array([len(im[2][0]) for im in imgs])
+    tuned, tune_ms = b.autotune(min(echoes, 200), spe, 16)
+    hidden = rng.uniform(2.0, 50.0, n_img)
+    fh = np.ones((n_img, 16))
+    fh[:, 0] = decrease_factor(hidden)
+    echo, _ = b.cpmg(fh, echoes, spe, derivatives=False)
+    bulk = np.exp(-echo_times(echoes, spe, 1.0 / 15.0) / t2b)
+    targets = echo[:, 0] / nwalk[:, None] * bulk + rng.normal(0.0, 1e-3, (n_img, echoes + 1))
+    rho0 = rng.uniform(2.0, 50.0, (n_img, 16))
+    fit = fit_rho_batch(b, targets, nwalk, echoes, spe, t2b, rho0, iters=args.fit_iters)
+    steps_per_pass = int(nwalk.sum()) * echoes * spe
+    # plain per-image CPMG: one walk per image per GA evaluation
+    eng = Engine(0)
+    per_image_s = []
+    for lab, blocks, w, por in imgs:
+        eng.upload_labels(lab, 1)
+        eng.upload_walkers(*w)
+        eng.cpmg(echoes, spe, 0.999)
+        per_image_s.append(eng.last_kernel_ms * 1e-3)
+    # GA evaluation count from one full GA run on the smallest image
+    k0 = int(np.argmin(nwalk * np.array([im[0].size for im in imgs])))
+    lab, blocks, w, por = imgs[k0]
+    eng.upload_labels(lab, 1)
+    eng.upload_walkers(*w)
+
+    def model(g):
+        m = eng.cpmg(echoes, spe, decrease_factor(g[0]))["echo_sum"]
+        return m / nwalk[k0] * bulk
+
+    ga = GeneticAlgorithm(misfit_fitness(model, targets[k0], 1e-3), [2.0], [50.0], population=64, seed=5)
+    ga.run(args.ga_generations)
+    ga_gpu = float(np.sum(per_image_s)) * ga.evaluations
+    line = {"metric": "GPU-seconds of the relaxivity fit over uneven images (batched+adjoint vs per-image CPMG+GA)",
+            "value": fit["gpu_seconds"], "unit": "GPU-s", "higher_is_better": False, "impl": "gb300",
+            "config": {"workload": args.workload, "images": n_img, "walkers_total": int(nwalk.sum()),
+                       "echoes": echoes, "steps_per_echo": spe, "candidates": 16,
+                       "walker_steps_per_pass": steps_per_pass, "autotuned_threads": tuned,
+                       "setup_seconds": setup_s},
+            "batched_fit": {"gpu_seconds": fit["gpu_seconds"], "passes": fit["walks"],
+                            "walker_steps_per_s_per_pass": steps_per_pass * fit["walks"] / fit["gpu_seconds"],
+                            "max_abs_rho_error": float(np.max(np.abs(fit["rho"] - hidden))),
+                            "median_abs_rho_error": float(np.median(np.abs(fit["rho"] - hidden)))},
+            "per_image_cpmg_ga": {"gpu_seconds_estimate": ga_gpu, "plain_walk_gpu_seconds_all_images":
+                                  float(np.sum(per_image_s)), "ga_evaluations_per_image": ga.evaluations,
+                                  "ga_generations": args.ga_generations, "population": 64,
+                                  "note": "GA GPU time = measured plain CPMG walk time of every image x the "
+                                          "evaluation count of a full GA run on the smallest image"},
+            "gpu_seconds_ratio_ga_over_batched": ga_gpu / max(fit["gpu_seconds"], 1e-12)}
+    print(json.dumps(line))
+    eng.close()
+    b.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -202,7 +342,14 @@ def main():
     ap.add_argument("--workload", default="cpmg-2phase-400")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--ga-generations", type=int, default=50)
+    ap.add_argument("--fit-evals", type=int, default=40)
+    ap.add_argument("--fit-iters", type=int, default=6)
     args = ap.parse_args()
+    if args.workload.startswith("rho-fit-multiphase"):
+        return run_fit_multiphase(args)
+    if args.workload.startswith("rho-fit-batch"):
+        return run_fit_batch(args)
     w = workload(args.workload)
     if args.impl == "reference":
         return run_reference(args, w)
