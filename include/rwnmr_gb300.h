@@ -86,6 +86,13 @@ rwnmr_status rwnmr_walkers_upload(rwnmr_ctx *ctx, int64_t n, const int32_t *x0, 
 rwnmr_status rwnmr_walkers_download(rwnmr_ctx *ctx, int32_t *x, int32_t *y, int32_t *z, uint64_t *seed,
                                     uint32_t *collisions);
 
+/* Per-walker decrease factors [n], each in [0, 1]: the reference's Walker::decreaseFactor when it
+ * differs between walkers (RHO_TYPE: sigmoid, where each walker's relaxivity follows from its
+ * collision rate; NMR_Simulation.cpp:1500-1508, Walker/walker.h:162-209). A CPMG or PFGSE walk
+ * whose params carry dfactor == NULL uses them; each walker's energy is then its own FP64 repeated
+ * product, as in Walker::walk_3D. Single-phase images only; uploading walkers clears them. */
+rwnmr_status rwnmr_walkers_set_dfactor(rwnmr_ctx *ctx, const double *dfactor);
+
 /* ---- CPMG walk ------------------------------------------------------------------------- */
 typedef struct rwnmr_cpmg_params
 {
@@ -94,7 +101,8 @@ typedef struct rwnmr_cpmg_params
     int32_t steps_per_echo; /* STEPS_PER_ECHO */
     int32_t n_echoes;       /* NMR_Simulation::numberOfEchoes */
     const double *dfactor;  /* [n_phases] collision decrease factor per phase,
-                               1 - (2/3) rho res / (D0 1e3)  (Walker/walker.h:203-209) */
+                               1 - (2/3) rho res / (D0 1e3)  (Walker/walker.h:203-209);
+                               NULL: the per-walker factors of rwnmr_walkers_set_dfactor */
     int32_t echoes_per_launch; /* 0 = automatic; bounds one kernel's duration */
 } rwnmr_cpmg_params;
 
@@ -114,6 +122,44 @@ rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, double *
  * grad_dfactor[p] = sum_e grad_echo[e] * d echo_sum[e] / d dfactor[p]. grad_echo: [n_echoes+1]. */
 rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, const double *grad_echo,
                                 double *grad_dfactor);
+
+/* ---- CPMG walk in an internal magnetic field ------------------------------------------- */
+/* The reference's RESIDUAL_FIELD option (NMR_cpmg.cpp:48-64 setInternalField;
+ * InternalField.cpp; CPMG_walk_{noflux,periodic,mirror}_field, NMR_cpmg_cuda.cpp:146-293,
+ * 409-567, 683-838). A field belongs to the uploaded image; uploading another image clears it. */
+
+/* Uniform field (RESIDUAL_FIELD: uniform): B = coord * gradient * 1e-6 * resolution in pore
+ * voxels and 0 in solid ones, coord the voxel index along direction 0/1/2 (x/y/z). Evaluated in
+ * the kernel; nothing is stored per voxel. */
+rwnmr_status rwnmr_field_set_uniform(rwnmr_ctx *ctx, double gradient, int32_t direction, double resolution);
+
+/* Arbitrary field (RESIDUAL_FIELD: import): count = nx*ny*nz doubles, x fastest, the layout of
+ * the reference's PATH_TO_FIELD file (InternalField::readDataFromFile). */
+rwnmr_status rwnmr_field_upload(rwnmr_ctx *ctx, const double *values, int64_t count);
+rwnmr_status rwnmr_field_clear(rwnmr_ctx *ctx);
+
+typedef struct rwnmr_field_cpmg_params
+{
+    int32_t bc;
+    int32_t shift;
+    int32_t steps_per_echo; /* each echo is two inversions of steps_per_echo / 2 steps */
+    int32_t n_echoes;
+    const double *dfactor;  /* [n_phases], or NULL for the per-walker factors */
+    double gamma;           /* 1e6 * gyromagnetic ratio (NMR_cpmg_cuda.cpp: gamma) */
+    double time_interval;   /* seconds per step (1e-3 * the walk's time step in ms) */
+    int32_t echoes_per_launch; /* 0 = automatic */
+} rwnmr_field_cpmg_params;
+
+/* Walks every walker from its initial state. Per step the phase gains gammatau * B before and
+ * after the move (gammatau = 0.5 * gamma * time_interval); an inversion negates it; a walker's
+ * energy after an echo is (prod over phases of f_p^collisions) * cos(phase). Outputs (nullable):
+ *   echo_sum  [n_echoes+1] energy sums (index 0 = initial), each walker's energy rounded to a
+ *             multiple of 2^-61 and summed exactly
+ *   phase_out [n]          final phase of every walker
+ * Final positions, seeds and collision counts are left in the context (rwnmr_walkers_download).
+ * Requires a field set by rwnmr_field_set_uniform or rwnmr_field_upload. */
+rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *ctx, const rwnmr_field_cpmg_params *p, double *echo_sum,
+                                  double *phase_out);
 
 /* ---- CPMG walk without allocation ------------------------------------------------------ */
 /* No counterpart in the reference (its CUDA path cudaMallocs its buffers on every run).

@@ -119,6 +119,40 @@ class Oracle:
             raise ValueError("orc_cpmg rejected its arguments")
         return out
 
+    def uniform_field(self, labels, resolution, gradient, direction):
+        im, keep = self.image(labels, 1)
+        out = np.zeros(np.asarray(labels).shape, np.float64)
+        self.lib.orc_uniform_field(ctypes.byref(im), ctypes.c_double(resolution), ctypes.c_double(gradient),
+                                   int(direction), _ptr(out))
+        return out
+
+    def cpmg_field(self, labels, walkers, n_echoes, steps_per_echo, dfactor, gammatau, field=None, dg=0.0, axis=0,
+                   bc="noflux", shift=0, threads=1, n_phases=None, walker_dfactor=None):
+        """Internal-field CPMG walk; field is a [nz][ny][nx] array or None for the uniform field
+        value = coord_axis * dg (0 in solid)."""
+        im, keep = self.image(labels, n_phases)
+        x0, y0, z0, s0 = [np.ascontiguousarray(a) for a in walkers]
+        n = len(x0)
+        P = im.n_phases
+        df = None if dfactor is None else np.ascontiguousarray(np.broadcast_to(np.asarray(dfactor, np.float64), (P,)))
+        wdf = None if walker_dfactor is None else np.ascontiguousarray(walker_dfactor, np.float64)
+        fld = None if field is None else np.ascontiguousarray(field, np.float64)
+        out = dict(
+            echo_fp64=np.zeros(n_echoes + 1), echo_fx=np.zeros((n_echoes + 1, 3), np.uint64),
+            xf=np.zeros(n, np.int32), yf=np.zeros(n, np.int32), zf=np.zeros(n, np.int32),
+            seedf=np.zeros(n, np.uint64), collf=np.zeros((n, P), np.uint32), phasef=np.zeros(n),
+        )
+        rc = self.lib.orc_cpmg_field(ctypes.byref(im), BC[bc], shift, ctypes.c_int64(n), _ptr(x0), _ptr(y0),
+                                     _ptr(z0), _ptr(s0), n_echoes, steps_per_echo,
+                                     None if df is None else _ptr(df), None if wdf is None else _ptr(wdf),
+                                     ctypes.c_double(gammatau), None if fld is None else _ptr(fld),
+                                     ctypes.c_double(dg), axis, _ptr(out["echo_fp64"]), _ptr(out["echo_fx"]),
+                                     _ptr(out["xf"]), _ptr(out["yf"]), _ptr(out["zf"]), _ptr(out["seedf"]),
+                                     _ptr(out["collf"]), _ptr(out["phasef"]), threads)
+        if rc != 0:
+            raise ValueError("orc_cpmg_field rejected its arguments")
+        return out
+
     def pfgse(self, labels, walkers, dfactor, steps, kvec, res, bc="noflux", shift=0, threads=1, n_phases=None):
         im, keep = self.image(labels, n_phases)
         x0, y0, z0, s0 = [np.ascontiguousarray(a) for a in walkers]
@@ -276,6 +310,20 @@ class RefSim:
             raise ValueError("cap too small")
         return dict(Mkt=Mkt[: nd * n_g].reshape(nd, n_g).copy(), steps=steps[:nd].copy(), dsat=dsat[:nd].copy(),
                     dmsd=dmsd[:nd].copy(), kvec=kvec.reshape(n_g, 3), delta=delta[:nd].copy())
+
+
+def ref_uniform_field(labels, resolution, gradient, direction):
+    """The reference's own uniform internal field (InternalField.cpp) for a binary image."""
+    lab = np.ascontiguousarray(np.asarray(labels) != 0, np.uint8)
+    nz, ny, nx = lab.shape
+    out = np.zeros(lab.shape, np.float64)
+    L = RefSim.lib()
+    L.ref_uniform_field.restype = ctypes.c_int
+    rc = L.ref_uniform_field(_ptr(lab), nx, ny, nz, ctypes.c_double(resolution), ctypes.c_double(gradient),
+                             int(direction), _ptr(out))
+    if rc != 0:
+        raise ValueError("ref_uniform_field failed")
+    return out
 
 
 def ref_bitblock(labels):

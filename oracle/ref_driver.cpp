@@ -28,6 +28,7 @@
 #include "NMR_Simulation/NMR_Simulation.h"
 #include "NMR_Simulation/NMR_cpmg.h"
 #include "NMR_Simulation/NMR_pfgse.h"
+#include "NMR_Simulation/InternalField.h"
 #include "Walker/walker.h"
 
 // ---------------------------------------------------------------------------------------------
@@ -447,9 +448,10 @@ int ref_pfgse(void *hv, double pulse_width, double gx, double gy, double gz, int
     return nd;
 }
 
-// The reference's bit-block packer on its own (BitBlock/bitBlock.cpp:138-221).
-// dims[3] <- blockColumns, blockRows, blockDepth; blocks sized by a first call with blocks == NULL.
-int ref_bitblock(const uint8_t *vox, int nx, int ny, int nz, uint64_t *blocks, int32_t *dims)
+} // extern "C"
+
+// Voxels [nz][ny][nx] (non-zero = solid) as the reference's image slices.
+static std::vector<cv::Mat> voxel_slices(const uint8_t *vox, int nx, int ny, int nz)
 {
     std::vector<cv::Mat> slices;
     for (int z = 0; z < nz; z++)
@@ -463,6 +465,16 @@ int ref_bitblock(const uint8_t *vox, int nx, int ny, int nz, uint64_t *blocks, i
         }
         slices.push_back(slice);
     }
+    return slices;
+}
+
+extern "C" {
+
+// The reference's bit-block packer on its own (BitBlock/bitBlock.cpp:138-221).
+// dims[3] <- blockColumns, blockRows, blockDepth; blocks sized by a first call with blocks == NULL.
+int ref_bitblock(const uint8_t *vox, int nx, int ny, int nz, uint64_t *blocks, int32_t *dims)
+{
+    std::vector<cv::Mat> slices = voxel_slices(vox, nx, ny, nz);
     BitBlock bb;
     bb.createBlockMap(slices);
     dims[0] = bb.blockColumns;
@@ -470,6 +482,20 @@ int ref_bitblock(const uint8_t *vox, int nx, int ny, int nz, uint64_t *blocks, i
     dims[2] = bb.blockDepth;
     if (blocks) std::memcpy(blocks, bb.blocks, sizeof(uint64_t) * (size_t)bb.numberOfBlocks);
     return bb.numberOfBlocks;
+}
+
+// The reference's uniform internal field (NMR_Simulation/InternalField.cpp: the
+// InternalField(BitBlock&, resolution, gradient, direction) constructor). out [nz][ny][nx].
+int ref_uniform_field(const uint8_t *vox, int nx, int ny, int nz, double resolution, double gradient, int direction,
+                      double *out)
+{
+    std::vector<cv::Mat> slices = voxel_slices(vox, nx, ny, nz);
+    BitBlock bb;
+    bb.createBlockMap(slices);
+    InternalField field(bb, resolution, gradient, direction);
+    if (field.getDimX() != nx || field.getDimY() != ny || field.getDimZ() != nz) return -1;
+    std::memcpy(out, field.getData(), sizeof(double) * (size_t)nx * ny * nz);
+    return 0;
 }
 
 } // extern "C"

@@ -132,6 +132,37 @@ inline int step(const orc_image &im, int bc, int shift, Walk &w)
     return (int)im.labels[((int64_t)iz * im.ny + iy) * im.nx + ix] - 1;
 }
 
+// Image voxel of a walk-grid position: pos >> shift for noflux (convertLocalToGlobal_CPMG), the
+// periodic / mirrored maps otherwise (NMR_cpmg_cuda.cpp:470-474, 749-751).
+inline void image_voxel(const orc_image &im, int bc, int shift, const Walk &w, int &ix, int &iy, int &iz)
+{
+    if (bc == ORC_BC_PERIODIC)
+    {
+        ix = map_periodic(w.x, shift, im.nx);
+        iy = map_periodic(w.y, shift, im.ny);
+        iz = map_periodic(w.z, shift, im.nz);
+    }
+    else if (bc == ORC_BC_MIRROR)
+    {
+        ix = map_mirror(w.x, shift, im.nx);
+        iy = map_mirror(w.y, shift, im.ny);
+        iz = map_mirror(w.z, shift, im.nz);
+    }
+    else
+    {
+        ix = w.x >> shift;
+        iy = w.y >> shift;
+        iz = w.z >> shift;
+    }
+}
+
+inline bool voxel_solid(const orc_image &im, int ix, int iy, int iz)
+{
+    int64_t block = (int64_t)(ix >> 2) + (int64_t)(iy >> 2) * im.bcols + (int64_t)(iz >> 2) * im.bcols * im.brows;
+    int bit = (ix & 3) + ((iy & 3) << 2) + ((iz & 3) << 4);
+    return ((im.blocks[block] >> bit) & 1ull) != 0;
+}
+
 inline uint64_t fxmul(uint64_t a, uint64_t b) { return (uint64_t)(((u128)a * (u128)b) >> 63); }
 
 struct Tables
@@ -296,6 +327,111 @@ int orc_cpmg(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const i
             for (int t = 0; t < nt; t++) s += acc_c[(size_t)t * n_echoes * P + k];
             echo_coll[k] = s;
         }
+    return 0;
+}
+
+void orc_uniform_field(const orc_image *img, double resolution, double gradient, int32_t direction, double *out)
+{
+    const double dg = gradient * (1.0e-6) * resolution; // InternalField.cpp: _gValue * (1.0e-6) * _resolution
+    for (int32_t z = 0; z < img->nz; z++)
+        for (int32_t y = 0; y < img->ny; y++)
+            for (int32_t x = 0; x < img->nx; x++)
+            {
+                const int coord = direction == 0 ? x : (direction == 1 ? y : z);
+                out[((int64_t)z * img->ny + y) * img->nx + x] = voxel_solid(*img, x, y, z) ? 0.0 : coord * dg;
+            }
+}
+
+int orc_cpmg_field(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const int32_t *x0, const int32_t *y0,
+                   const int32_t *z0, const uint64_t *seed0, int32_t n_echoes, int32_t steps_per_echo,
+                   const double *dfactor, const double *walker_dfactor, double gammatau, const double *field,
+                   double dg, int32_t axis, double *echo_fp64, uint64_t *echo_fx, int32_t *xf, int32_t *yf,
+                   int32_t *zf, uint64_t *seedf, uint32_t *collf, double *phasef, int32_t threads)
+{
+    if (!image_ok(img) || n < 0 || n_echoes < 0 || steps_per_echo < 1 || shift < 0 || axis < 0 || axis > 2)
+        return -1;
+    if (!dfactor && !(walker_dfactor && img->n_phases == 1)) return -1;
+    const double one = 1.0;
+    if (!dfactor) dfactor = &one; // tables unused
+    const int P = img->n_phases;
+    const int32_t spi = steps_per_echo / 2; // stepsPerInversion
+    Tables tab;
+    tab.build(dfactor, P, n_echoes * 2 * spi);
+    const int nt = threads > 1 ? threads : 1;
+    const size_t E1 = (size_t)n_echoes + 1;
+    std::vector<double> acc_fp((size_t)nt * E1, 0.0);
+    std::vector<uint64_t> acc_fx((size_t)nt * E1 * 3, 0);
+    // field value at the walker's voxel (the array, or the uniform field evaluated in place)
+    auto field_at = [&](const Walk &w) {
+        int ix, iy, iz;
+        image_voxel(*img, bc, shift, w, ix, iy, iz);
+        if (field) return field[((int64_t)iz * img->ny + iy) * img->nx + ix];
+        const int coord = axis == 0 ? ix : (axis == 1 ? iy : iz);
+        return voxel_solid(*img, ix, iy, iz) ? 0.0 : coord * dg;
+    };
+    auto energy_fx = [](double e) { return (uint64_t)((int64_t)std::nearbyint(std::ldexp(e, 61)) + (1ll << 61)); };
+
+#pragma omp parallel num_threads(nt)
+    {
+        int t = omp_get_thread_num();
+        int64_t lo = n * t / nt, hi = n * (t + 1) / nt;
+        double *afp = &acc_fp[(size_t)t * E1];
+        uint64_t *afx = &acc_fx[(size_t)t * E1 * 3];
+        std::vector<uint32_t> c(P);
+        for (int64_t i = lo; i < hi; i++)
+        {
+            Walk w{x0[i], y0[i], z0[i], seed0[i]};
+            std::fill(c.begin(), c.end(), 0u);
+            double phase = 0.0;
+            double palive = 1.0; // per-walker factors: the reference's running product
+            const double fw = walker_dfactor ? walker_dfactor[i] : 1.0;
+            auto survival = [&]() { return walker_dfactor ? palive : tab.energy(c.data()); };
+            double e0 = survival() * std::cos(phase);
+            afp[0] += e0;
+            add_limbs(afx, energy_fx(e0));
+            for (int32_t e = 0; e < n_echoes; e++)
+            {
+                for (int inv = 0; inv < 2; inv++)
+                {
+                    phase = -phase;
+                    for (int32_t s = 0; s < spi; s++)
+                    {
+                        phase = std::fma(gammatau, field_at(w), phase);
+                        int ph = step(*img, bc, shift, w);
+                        if (ph >= 0)
+                        {
+                            c[ph]++;
+                            palive = palive * fw;
+                        }
+                        phase = std::fma(gammatau, field_at(w), phase);
+                    }
+                }
+                const double en = survival() * std::cos(phase);
+                afp[e + 1] += en;
+                add_limbs(&afx[(size_t)(e + 1) * 3], energy_fx(en));
+            }
+            if (xf) xf[i] = w.x;
+            if (yf) yf[i] = w.y;
+            if (zf) zf[i] = w.z;
+            if (seedf) seedf[i] = w.seed;
+            if (collf)
+                for (int q = 0; q < P; q++) collf[(size_t)i * P + q] = c[q];
+            if (phasef) phasef[i] = phase;
+        }
+    }
+    for (size_t e = 0; e < E1; e++)
+    {
+        double s = 0.0;
+        uint64_t f[3] = {0, 0, 0};
+        for (int t = 0; t < nt; t++)
+        {
+            s += acc_fp[(size_t)t * E1 + e];
+            for (int k = 0; k < 3; k++) f[k] += acc_fx[((size_t)t * E1 + e) * 3 + k];
+        }
+        if (echo_fp64) echo_fp64[e] = s;
+        if (echo_fx)
+            for (int k = 0; k < 3; k++) echo_fx[e * 3 + k] = f[k];
+    }
     return 0;
 }
 

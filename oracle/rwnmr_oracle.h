@@ -67,6 +67,31 @@ int orc_pfgse(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const 
               int32_t n_g, const double *kvec, double res, double *M, double *esum, uint64_t *msd, uint64_t *esum_fx,
               int32_t threads);
 
+/* The reference's uniform internal field (NMR_Simulation/InternalField.cpp, fillDataArray):
+ * out[(z*ny + y)*nx + x] = coord * dG in pore voxels and 0 in solid ones, coord the voxel's
+ * x, y or z (direction 0/1/2) and dG = gradient * 1e-6 * resolution. */
+void orc_uniform_field(const orc_image *img, double resolution, double gradient, int32_t direction, double *out);
+
+/* CPMG walk in an internal magnetic field (NMR_cpmg_cuda.cpp:146-293 noflux, 409-567 periodic,
+ * 683-838 mirror). Each echo is two inversions of steps_per_echo/2 steps; an inversion negates
+ * the phase, and every step adds gammatau * field at the walker's voxel before and after the
+ * move, each addition one fused multiply-add (nvcc's contraction of `phase += gammatau *
+ * field[i]`). A rejected move counts a collision on the solid's phase; the walker's energy after
+ * an echo is prod_p T_p[c_p] * cos(phase).
+ *   field        [nz][ny][nx] values at image voxels, or NULL for the uniform field of
+ *                orc_uniform_field with dG = dg along axis `axis`, evaluated voxel by voxel
+ *   walker_dfactor  [n] per-walker decrease factors (single phase: pAlive *= f_w per collision,
+ *                the reference's own update), or NULL for the per-phase tables of dfactor
+ *   echo_fp64    [n_echoes+1] serial FP64 sum of walker energies
+ *   echo_fx      [(n_echoes+1)*3] limb sums (bits 0-20, 21-41, 42-62) of round(E * 2^61) + 2^61
+ *   final state  positions, seeds, collisions [n*n_phases], phases [n]
+ * Any output may be NULL. Returns 0, or -1 on bad arguments. */
+int orc_cpmg_field(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const int32_t *x0, const int32_t *y0,
+                   const int32_t *z0, const uint64_t *seed0, int32_t n_echoes, int32_t steps_per_echo,
+                   const double *dfactor, const double *walker_dfactor, double gammatau, const double *field,
+                   double dg, int32_t axis, double *echo_fp64, uint64_t *echo_fx, int32_t *xf, int32_t *yf,
+                   int32_t *zf, uint64_t *seedf, uint32_t *collf, double *phasef, int32_t threads);
+
 /* Per-walker displacements after a PFGSE-style walk of `steps` steps (for histogram checks). */
 int orc_displacements(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const int32_t *x0,
                       const int32_t *y0, const int32_t *z0, const uint64_t *seed0, int32_t steps, int32_t *dx,

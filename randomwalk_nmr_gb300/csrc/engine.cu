@@ -88,6 +88,8 @@ struct rwnmr_ctx
 
     int64_t n = 0;
     bool has_walkers = false;
+    bool has_wf = false; // per-walker decrease factors uploaded
+    DevBuf<double> wf, wenergy;
     DevBuf<int32_t> x0, y0, z0, x, y, z;
     DevBuf<uint64_t> seed0, seed;
     DevBuf<uint32_t> coll;
@@ -99,6 +101,12 @@ struct rwnmr_ctx
     DevBuf<double> grad, partial, partial_g, kbuf, Mbuf, gbuf;
     DevBuf<int32_t> ibuf, disp;
     DevBuf<double> energy;
+
+    // internal field: 0 none, 1 uniform (evaluated in the kernel), 2 array
+    int field_mode = 0;
+    double field_dg = 0.0;
+    int field_axis = 0;
+    DevBuf<double> field, phase;
 
     rwnmr_status fail(rwnmr_status s, const char *fmt, ...)
     {
@@ -172,6 +180,15 @@ rwnmr_status check_geom(rwnmr_ctx *ctx, int bc, int shift)
 {
     if (bc < RWNMR_BC_NOFLUX || bc > RWNMR_BC_MIRROR) return ctx->fail(RWNMR_ERR_INVALID, "unknown boundary condition %d", bc);
     if (shift < 0 || shift > 10) return ctx->fail(RWNMR_ERR_INVALID, "voxel-division shift %d out of range 0..10", shift);
+    return RWNMR_OK;
+}
+
+// dfactor == NULL selects the per-walker decrease factors (single-phase images).
+rwnmr_status check_walker_dfactor(rwnmr_ctx *ctx)
+{
+    if (!ctx->has_wf) return ctx->fail(RWNMR_ERR_STATE, "dfactor is NULL and no per-walker decrease factors are set");
+    if (ctx->n_phases != 1)
+        return ctx->fail(RWNMR_ERR_UNSUPPORTED, "per-walker decrease factors need a single-phase image");
     return RWNMR_OK;
 }
 
@@ -272,6 +289,7 @@ static rwnmr_status set_dims(rwnmr_ctx *c, int32_t nx, int32_t ny, int32_t nz, i
     c->bdepth = (nz + 3) / 4;
     c->n_phases = n_phases;
     c->words = words_for(n_phases);
+    c->field_mode = 0; // a field belongs to the image it was set for
     return RWNMR_OK;
 }
 
@@ -358,6 +376,7 @@ rwnmr_status rwnmr_walkers_upload(rwnmr_ctx *c, int64_t n, const int32_t *x0, co
     if (n < 0 || n > (1ll << 31) - 1) return c->fail(RWNMR_ERR_INVALID, "walker count %lld out of range", (long long)n);
     if (n > 0 && (!x0 || !y0 || !z0 || !seed0)) return c->fail(RWNMR_ERR_INVALID, "walker arrays must not be NULL");
     c->has_walkers = false;
+    c->has_wf = false;
     cudaSetDevice(c->device);
     const size_t m = (size_t)std::max<int64_t>(n, 1);
     RW_CUDA(c, c->x0.ensure(m), "walkers"); RW_CUDA(c, c->y0.ensure(m), "walkers"); RW_CUDA(c, c->z0.ensure(m), "walkers");
@@ -408,6 +427,24 @@ rwnmr_status rwnmr_walkers_download(rwnmr_ctx *c, int32_t *x, int32_t *y, int32_
     return RWNMR_OK;
 }
 
+rwnmr_status rwnmr_walkers_set_dfactor(rwnmr_ctx *c, const double *dfactor)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    if (!c->has_walkers) return c->fail(RWNMR_ERR_STATE, "no walkers uploaded");
+    if (c->n > 0 && !dfactor) return c->fail(RWNMR_ERR_INVALID, "dfactor is NULL");
+    for (int64_t i = 0; i < c->n; i++)
+        if (!(dfactor[i] >= 0.0 && dfactor[i] <= 1.0))
+            return c->fail(RWNMR_ERR_UNSUPPORTED, "decrease factor %g of walker %lld outside [0, 1]", dfactor[i], (long long)i);
+    cudaSetDevice(c->device);
+    RW_CUDA(c, c->wf.ensure((size_t)std::max<int64_t>(c->n, 1)), "walker decrease factors");
+    if (c->n > 0)
+        RW_CUDA(c, cudaMemcpyAsync(c->wf.p, dfactor, (size_t)c->n * 8, cudaMemcpyHostToDevice, c->stream),
+                "walker decrease factors");
+    RW_CUDA(c, cudaStreamSynchronize(c->stream), "walker decrease factors");
+    c->has_wf = true;
+    return RWNMR_OK;
+}
+
 // ---- CPMG -------------------------------------------------------------------------------------
 rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *echo_sum, uint64_t *echo_fx,
                             uint64_t *echo_coll)
@@ -415,18 +452,24 @@ rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *ec
     RW_TRY(need_run_state(c));
     if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
     RW_TRY(check_geom(c, p->bc, p->shift));
-    RW_TRY(check_dfactor(c, p->dfactor));
+    const bool per_walker = p->dfactor == nullptr;
+    RW_TRY(per_walker ? check_walker_dfactor(c) : check_dfactor(c, p->dfactor));
     if (p->n_echoes < 0 || p->steps_per_echo < 1) return c->fail(RWNMR_ERR_INVALID, "bad echo count / steps per echo");
     const int64_t nmax = (int64_t)p->n_echoes * p->steps_per_echo;
     if (nmax > (1ll << 28)) return c->fail(RWNMR_ERR_UNSUPPORTED, "walk of %lld steps too long", (long long)nmax);
     cudaSetDevice(c->device);
     const int slots = phase_slots(c->n_phases);
     const int K = 3 + slots;
-    std::vector<uint64_t> fx;
-    build_tables(p->dfactor, c->n_phases, slots, nmax, nullptr, &fx);
-    RW_CUDA(c, c->tfx.ensure(fx.size()), "tables");
+    if (per_walker)
+        RW_CUDA(c, c->wenergy.ensure((size_t)std::max<int64_t>(c->n, 1)), "walker energies");
+    else
+    {
+        std::vector<uint64_t> fx;
+        build_tables(p->dfactor, c->n_phases, slots, nmax, nullptr, &fx);
+        RW_CUDA(c, c->tfx.ensure(fx.size()), "tables");
+        RW_CUDA(c, cudaMemcpyAsync(c->tfx.p, fx.data(), fx.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables upload");
+    }
     RW_CUDA(c, c->acc.ensure((size_t)(p->n_echoes + 1) * K), "echo accumulators");
-    RW_CUDA(c, cudaMemcpyAsync(c->tfx.p, fx.data(), fx.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables upload");
     RW_CUDA(c, cudaMemsetAsync(c->acc.p, 0, (size_t)(p->n_echoes + 1) * K * 8, c->stream), "accumulator reset");
     RW_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(unsigned), c->stream), "status reset");
 
@@ -436,8 +479,10 @@ rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *ec
     CpmgLaunch L{};
     L.steps_per_echo = p->steps_per_echo;
     L.record = 1;
-    L.tfx = c->tfx.p;
+    L.tfx = per_walker ? nullptr : c->tfx.p;
     L.tstride = (int)(nmax + 1);
+    L.wf = per_walker ? c->wf.p : nullptr;
+    L.wenergy = per_walker ? c->wenergy.p : nullptr;
     L.acc = c->acc.p;
     L.status = c->status.p;
     RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
@@ -479,10 +524,134 @@ rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *ec
     return RWNMR_OK;
 }
 
+// ---- internal field ---------------------------------------------------------------------------
+rwnmr_status rwnmr_field_set_uniform(rwnmr_ctx *c, double gradient, int32_t direction, double resolution)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    if (!c->has_image) return c->fail(RWNMR_ERR_STATE, "no image uploaded");
+    if (direction < 0 || direction > 2) return c->fail(RWNMR_ERR_INVALID, "gradient direction %d not in 0..2", direction);
+    if (!std::isfinite(gradient) || !std::isfinite(resolution))
+        return c->fail(RWNMR_ERR_INVALID, "gradient and resolution must be finite");
+    c->field_dg = gradient * (1.0e-6) * resolution; // InternalField::fillDataArray
+    c->field_axis = direction;
+    c->field_mode = 1;
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_field_upload(rwnmr_ctx *c, const double *values, int64_t count)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    if (!c->has_image) return c->fail(RWNMR_ERR_STATE, "no image uploaded");
+    const int64_t vol = (int64_t)c->nx * c->ny * c->nz;
+    if (!values || count != vol)
+        return c->fail(RWNMR_ERR_INVALID, "field has %lld values, the image %lld voxels", (long long)count, (long long)vol);
+    cudaSetDevice(c->device);
+    RW_CUDA(c, c->field.ensure((size_t)vol), "field");
+    RW_CUDA(c, cudaMemcpyAsync(c->field.p, values, (size_t)vol * 8, cudaMemcpyHostToDevice, c->stream), "field upload");
+    RW_CUDA(c, cudaStreamSynchronize(c->stream), "field upload");
+    c->field_mode = 2;
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_field_clear(rwnmr_ctx *c)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    c->field_mode = 0;
+    c->field.release();
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p, double *echo_sum, double *phase_out)
+{
+    RW_TRY(need_run_state(c));
+    if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
+    if (c->field_mode == 0) return c->fail(RWNMR_ERR_STATE, "no internal field set");
+    RW_TRY(check_geom(c, p->bc, p->shift));
+    const bool per_walker = p->dfactor == nullptr;
+    RW_TRY(per_walker ? check_walker_dfactor(c) : check_dfactor(c, p->dfactor));
+    if (p->n_echoes < 0 || p->steps_per_echo < 1) return c->fail(RWNMR_ERR_INVALID, "bad echo count / steps per echo");
+    if (!std::isfinite(p->gamma) || !std::isfinite(p->time_interval))
+        return c->fail(RWNMR_ERR_INVALID, "gamma and time interval must be finite");
+    const int spi = p->steps_per_echo / 2;
+    const int64_t nmax = (int64_t)p->n_echoes * 2 * spi;
+    if (nmax > (1ll << 28)) return c->fail(RWNMR_ERR_UNSUPPORTED, "walk of %lld steps too long", (long long)nmax);
+    cudaSetDevice(c->device);
+    const int slots = phase_slots(c->n_phases);
+    constexpr int K = 3;
+    if (per_walker)
+        RW_CUDA(c, c->wenergy.ensure((size_t)std::max<int64_t>(c->n, 1)), "walker survival probabilities");
+    else
+    {
+        std::vector<double> t;
+        build_tables(p->dfactor, c->n_phases, slots, nmax, &t, nullptr);
+        RW_CUDA(c, c->tfp.ensure(t.size()), "tables");
+        RW_CUDA(c, cudaMemcpyAsync(c->tfp.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables upload");
+    }
+    RW_CUDA(c, c->acc.ensure((size_t)(p->n_echoes + 1) * K), "echo accumulators");
+    RW_CUDA(c, c->phase.ensure((size_t)std::max<int64_t>(c->n, 1)), "walker phases");
+    RW_CUDA(c, cudaMemsetAsync(c->acc.p, 0, (size_t)(p->n_echoes + 1) * K * 8, c->stream), "accumulator reset");
+    RW_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(unsigned), c->stream), "status reset");
+
+    const int chunk = p->echoes_per_launch > 0 ? p->echoes_per_launch
+                                               : std::max(32, (4096 / std::max(1, 2 * spi)) / 32 * 32);
+    const DevImage im = c->image(p->bc, p->shift);
+    const WalkState st = c->state();
+    FieldLaunch L{};
+    L.steps_per_inversion = spi;
+    L.t = per_walker ? nullptr : c->tfp.p;
+    L.tstride = (int)(nmax + 1);
+    L.wf = per_walker ? c->wf.p : nullptr;
+    L.palive = per_walker ? c->wenergy.p : nullptr;
+    L.gammatau = 0.5 * p->gamma * p->time_interval; // NMR_cpmg_cuda.cpp: gammatau = 0.5*gamma*timeInterval
+    L.field = c->field_mode == 2 ? c->field.p : nullptr;
+    L.dg = c->field_dg;
+    L.axis = c->field_axis;
+    L.phase = c->phase.p;
+    L.acc = c->acc.p;
+    L.status = c->status.p;
+    const bool uniform = c->field_mode == 1;
+    RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
+    if (c->n > 0)
+    {
+        for (int e = 0; e < std::max(p->n_echoes, 1); e += chunk)
+        {
+            L.e_begin = e;
+            L.e_end = std::min(p->n_echoes, e + chunk);
+            L.from_initial = e == 0;
+            RW_CUDA(c, launch_cpmg_field(bc_key(p->bc, p->shift), slots, uniform, im, st, L, walk_grid(c->n), c->stream),
+                    "field cpmg kernel");
+            c->launches++;
+        }
+    }
+    RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
+    std::vector<unsigned long long> acc((size_t)(p->n_echoes + 1) * K);
+    RW_CUDA(c, cudaMemcpyAsync(acc.data(), c->acc.p, acc.size() * 8, cudaMemcpyDeviceToHost, c->stream), "echo readback");
+    if (phase_out && c->n > 0)
+        RW_CUDA(c, cudaMemcpyAsync(phase_out, c->phase.p, (size_t)c->n * 8, cudaMemcpyDeviceToHost, c->stream),
+                "phase readback");
+    RW_TRY(c->check_status("field cpmg walk"));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->last_ms = ms;
+    if (echo_sum)
+    {
+        // every walker added round(E * 2^61) + 2^61
+        const __int128 offset = (__int128)c->n << 61;
+        for (int e = 0; e <= p->n_echoes; e++)
+        {
+            const unsigned long long *a = &acc[(size_t)e * K];
+            const __int128 v = (__int128)a[0] + ((__int128)a[1] << 21) + ((__int128)a[2] << 42) - offset;
+            echo_sum[e] = std::ldexp((double)v, -61);
+        }
+    }
+    return RWNMR_OK;
+}
+
 rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const double *grad_echo, double *grad_dfactor)
 {
     RW_TRY(need_run_state(c));
     if (!p || !grad_echo || !grad_dfactor) return c->fail(RWNMR_ERR_INVALID, "NULL argument");
+    if (!p->dfactor) return c->fail(RWNMR_ERR_UNSUPPORTED, "the adjoint differentiates per-phase decrease factors");
     RW_TRY(check_geom(c, p->bc, p->shift));
     RW_TRY(check_dfactor(c, p->dfactor));
     if (p->n_echoes < 0 || p->steps_per_echo < 1) return c->fail(RWNMR_ERR_INVALID, "bad echo count / steps per echo");
@@ -623,7 +792,8 @@ static rwnmr_status pfgse_impl(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double
     RW_TRY(need_run_state(c));
     if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
     RW_TRY(check_geom(c, p->bc, p->shift));
-    RW_TRY(check_dfactor(c, p->dfactor));
+    const bool per_walker = p->dfactor == nullptr;
+    RW_TRY(per_walker ? check_walker_dfactor(c) : check_dfactor(c, p->dfactor));
     if (p->n_delta < 0 || p->n_g < 0 || (p->n_delta > 0 && !p->steps) || (p->n_g > 0 && !p->kvec))
         return c->fail(RWNMR_ERR_INVALID, "bad PFGSE sizes");
     for (int i = 0; i < p->n_delta; i++)
@@ -653,16 +823,22 @@ static rwnmr_status pfgse_impl(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double
     const int slots = phase_slots(c->n_phases);
     std::vector<uint64_t> fx;
     std::vector<double> t;
-    build_tables(p->dfactor, c->n_phases, slots, smax, axis < 0 ? &t : nullptr, &fx);
+    if (!per_walker) build_tables(p->dfactor, c->n_phases, slots, smax, axis < 0 ? &t : nullptr, &fx);
     const int nd = p->n_delta, ng = p->n_g;
     const int hh = smax;
     const size_t nbins = 2 * (size_t)hh + 1;
-    RW_CUDA(c, c->tfx.ensure(fx.size()), "tables");
-    RW_CUDA(c, cudaMemcpyAsync(c->tfx.p, fx.data(), fx.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables");
+    if (!per_walker)
+    {
+        RW_CUDA(c, c->tfx.ensure(fx.size()), "tables");
+        RW_CUDA(c, cudaMemcpyAsync(c->tfx.p, fx.data(), fx.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables");
+    }
     if (axis < 0)
     {
-        RW_CUDA(c, c->tfp.ensure(t.size()), "tables");
-        RW_CUDA(c, cudaMemcpyAsync(c->tfp.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables");
+        if (!per_walker)
+        {
+            RW_CUDA(c, c->tfp.ensure(t.size()), "tables");
+            RW_CUDA(c, cudaMemcpyAsync(c->tfp.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables");
+        }
         RW_CUDA(c, c->disp.ensure((size_t)std::max(nd, 1) * std::max<int64_t>(c->n, 1) * 3), "displacements");
         RW_CUDA(c, c->energy.ensure((size_t)std::max(nd, 1) * std::max<int64_t>(c->n, 1)), "energies");
     }
@@ -689,6 +865,7 @@ static rwnmr_status pfgse_impl(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double
     L.hist = c->hist.p;
     L.disp = c->disp.p;
     L.energy = c->energy.p;
+    L.wf = per_walker ? c->wf.p : nullptr;
     L.status = c->status.p;
     RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
     if (c->n > 0 && nd > 0)

@@ -1,0 +1,247 @@
+// CPMG walk in an internal magnetic field (sm_103a).
+//
+// Reference semantics (NMR_cpmg_cuda.cpp:146-293 noflux, 409-567 periodic, 683-838 mirror; the
+// field itself NMR_Simulation/InternalField.cpp):
+//   * an echo is two inversions of steps_per_echo / 2 steps (an odd step count loses a step);
+//   * an inversion negates the walker's phase;
+//   * every step adds gammatau * B at the walker's image voxel before and after the move, each
+//     addition a fused multiply-add (nvcc contracts the reference's `phase += gammatau * B`);
+//   * a rejected move multiplies the survival probability pAlive by the decrease factor;
+//   * after each echo the walker's energy is pAlive * cos(phase).
+// GB300 formulation:
+//   * pAlive is the FP64 table T[c] of the collision count, the reference's repeated product bit
+//     for bit (a product over phases for multi-phase images);
+//   * B at the walker's voxel lives in a register and is refreshed only after a move; the
+//     uniform field (coord * dG in pore voxels, 0 in solid ones) is evaluated in place rather
+//     than gathered from an 8-byte-per-voxel array;
+//   * energies are signed: each walker adds round(E * 2^61) + 2^61, in [0, 2^62], as three 21-bit
+//     limbs through redux.sync (the same echo-transposed accumulation as the plain CPMG walk), and
+//     the host subtracts n * 2^61. Sums are exact integers, identical run to run.
+#include <cstdint>
+#include <type_traits>
+#include <cuda_runtime.h>
+
+#include "walk_device.cuh"
+#include "walk_kernels.cuh"
+
+namespace rwnmr
+{
+
+namespace
+{
+constexpr unsigned FULL = 0xffffffffu;
+constexpr uint64_t M21 = (1ull << 21) - 1;
+
+template <int BC, int W, bool UNIFORM>
+__device__ __forceinline__ double field_at(const DevImage &im, const WalkerPos &p, const FieldLaunch &L,
+                                           bool may_be_solid)
+{
+    int ix, iy, iz;
+    current_voxel<BC>(im, p, ix, iy, iz);
+    if (UNIFORM)
+    {
+        // a walker only ever moves into pore voxels; only its start voxel can be solid
+        if (may_be_solid && voxel_solid<W>(im, ix, iy, iz)) return 0.0;
+        const int coord = L.axis == 0 ? ix : (L.axis == 1 ? iy : iz);
+        return (double)coord * L.dg;
+    }
+    return __ldg(L.field + ((int64_t)ix + (int64_t)iy * im.nx + (int64_t)iz * im.nx * im.ny));
+}
+
+__device__ __forceinline__ uint64_t energy_offset_fx(double e)
+{
+    return (uint64_t)(__double2ll_rn(e * 0x1p61) + (1ll << 61));
+}
+} // namespace
+
+// WF (single phase): per-walker decrease factors; pAlive is then the walker's own running FP64
+// product, one multiply per collision, exactly the reference's `local_pAlive *= local_dFactor`.
+template <int BC, int NP, bool UNIFORM, bool WF>
+__global__ void __launch_bounds__(kWalkThreads) cpmg_field_kernel(DevImage im, WalkState st, FieldLaunch L)
+{
+    static_assert(!WF || NP == 1, "per-walker decrease factors are for single-phase images");
+    constexpr int W = WordsPerBlock<NP>::value;
+    constexpr int K = 3;
+    __shared__ unsigned long long sacc[32 * K];
+
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool active = i < st.n;
+
+    WalkerPos p{};
+    uint64_t seed = 0;
+    uint32_t c[NP];
+#pragma unroll
+    for (int q = 0; q < NP; q++) c[q] = 0;
+    double phase = 0.0;
+    double fw = 1.0, pa = 1.0; // WF: decrease factor and survival probability
+    if (active)
+    {
+        if (WF)
+        {
+            fw = L.wf[i];
+            pa = L.from_initial ? 1.0 : L.palive[i];
+        }
+        if (L.from_initial)
+        {
+            p.x = st.x0[i];
+            p.y = st.y0[i];
+            p.z = st.z0[i];
+            seed = st.seed0[i];
+        }
+        else
+        {
+            p.x = st.x[i];
+            p.y = st.y[i];
+            p.z = st.z[i];
+            seed = st.seed[i];
+#pragma unroll
+            for (int q = 0; q < NP; q++) c[q] = st.coll[(size_t)q * st.n + i];
+            phase = L.phase[i];
+        }
+        if (!start_ok<BC>(im, p))
+        {
+            atomicOr(L.status, kStatusBadStart);
+            active = false;
+        }
+        init_image_coords<BC>(im, p);
+    }
+    const double B0 = active ? field_at<BC, W, UNIFORM>(im, p, L, true) : 0.0;
+    double B = B0;
+
+    for (int k = threadIdx.x; k < 32 * K; k += blockDim.x) sacc[k] = 0;
+    if (L.e_begin == 0)
+    {
+        // initial energy sum (output index 0)
+        const double pal = WF ? pa : energy_fp64<NP>(L.t, L.tstride, c);
+        const uint64_t u = active ? energy_offset_fx(pal * cos(phase)) : 0;
+        const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(u & M21));
+        const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((u >> 21) & M21));
+        const uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(u >> 42));
+        if (lane == 0)
+        {
+            atomicAdd(&L.acc[0], (unsigned long long)r0);
+            atomicAdd(&L.acc[1], (unsigned long long)r1);
+            atomicAdd(&L.acc[2], (unsigned long long)r2);
+        }
+    }
+    __syncthreads();
+
+    for (int e0 = L.e_begin; e0 < L.e_end; e0 += 32)
+    {
+        const int e1 = min(e0 + 32, L.e_end);
+        uint32_t keep[K] = {0, 0, 0};
+        for (int e = e0; e < e1; e++)
+        {
+            uint64_t u = 0;
+            if (active)
+            {
+#pragma unroll 1
+                for (int inv = 0; inv < 2; inv++)
+                {
+                    phase = -phase;
+                    for (int s = 0; s < L.steps_per_inversion; s++)
+                    {
+                        phase = __fma_rn(L.gammatau, B, phase);
+                        bool wall;
+                        int ph;
+                        walker_step<BC, W>(im, p, seed, wall, ph);
+                        if (wall)
+                        {
+#pragma unroll
+                            for (int q = 0; q < NP; q++) c[q] += (ph == q) ? 1u : 0u;
+                            if (WF) pa = pa * fw;
+                        }
+                        else
+                        {
+                            B = field_at<BC, W, UNIFORM>(im, p, L, false);
+                        }
+                        phase = __fma_rn(L.gammatau, B, phase);
+                    }
+                }
+                u = energy_offset_fx((WF ? pa : energy_fp64<NP>(L.t, L.tstride, c)) * cos(phase));
+            }
+            const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(u & M21));
+            const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((u >> 21) & M21));
+            const uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(u >> 42));
+            const bool mine = lane == (e - e0);
+            keep[0] = mine ? r0 : keep[0];
+            keep[1] = mine ? r1 : keep[1];
+            keep[2] = mine ? r2 : keep[2];
+        }
+        // lane l holds this warp's sums for echo e0 + l
+        if (lane < e1 - e0)
+        {
+#pragma unroll
+            for (int k = 0; k < K; k++)
+                if (keep[k]) atomicAdd(&sacc[lane * K + k], (unsigned long long)keep[k]);
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < (e1 - e0) * K; k += blockDim.x)
+        {
+            unsigned long long v = sacc[k];
+            if (v) atomicAdd(&L.acc[(size_t)(e0 + 1 + k / K) * K + (k % K)], v);
+            sacc[k] = 0;
+        }
+        __syncthreads();
+    }
+
+    if (active)
+    {
+        st.x[i] = p.x;
+        st.y[i] = p.y;
+        st.z[i] = p.z;
+        st.seed[i] = seed;
+#pragma unroll
+        for (int q = 0; q < NP; q++) st.coll[(size_t)q * st.n + i] = c[q];
+        L.phase[i] = phase;
+        if (WF) L.palive[i] = pa;
+    }
+}
+
+namespace
+{
+template <typename F>
+void with_bc_field(int bc_key, F &&f)
+{
+    switch (bc_key)
+    {
+    case BC_NOFLUX: f(std::integral_constant<int, BC_NOFLUX>{}); break;
+    case BC_PERIODIC: f(std::integral_constant<int, BC_PERIODIC>{}); break;
+    case BC_MIRROR: f(std::integral_constant<int, BC_MIRROR>{}); break;
+    default: f(std::integral_constant<int, BC_GENERIC>{}); break;
+    }
+}
+} // namespace
+
+cudaError_t launch_cpmg_field(int bc_key, int np, bool uniform, const DevImage &im, const WalkState &st,
+                              const FieldLaunch &L, dim3 grid, cudaStream_t s)
+{
+    auto go = [&](auto npc) {
+        constexpr int NP = decltype(npc)::value;
+        with_bc_field(bc_key, [&](auto bcc) {
+            constexpr int BC = decltype(bcc)::value;
+            if constexpr (NP == 1)
+            {
+                if (L.wf)
+                {
+                    if (uniform)
+                        cpmg_field_kernel<BC, 1, true, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    else
+                        cpmg_field_kernel<BC, 1, false, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    return;
+                }
+            }
+            if (uniform)
+                cpmg_field_kernel<BC, NP, true, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            else
+                cpmg_field_kernel<BC, NP, false, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+        });
+    };
+    if (np == 1) go(std::integral_constant<int, 1>{});
+    else if (np == 2) go(std::integral_constant<int, 2>{});
+    else go(std::integral_constant<int, 4>{});
+    return cudaGetLastError();
+}
+
+} // namespace rwnmr

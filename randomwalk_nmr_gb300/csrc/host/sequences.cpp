@@ -262,6 +262,43 @@ double Simulation::decrease_factor(double rho) const
     return 1.0 - (2.0 / 3.0) * ((rho * voxel_res) / (rw.d0 * 1e03));
 }
 
+double Simulation::sigmoid_rho(double xi) const
+{
+    // two sigmoids K + (A - K) / (1 + exp(-B (xi - eps))) (Walker/walker.h:174-196)
+    const std::vector<double> &p = rw.rho;
+    const double s1 = p[1] + ((p[0] - p[1]) / (1 + std::exp((-1) * p[3] * (xi - p[2]))));
+    const double s2 = p[5] + ((p[4] - p[5]) / (1 + std::exp((-1) * p[7] * (xi - p[6]))));
+    return s1 + s2;
+}
+
+bool Simulation::upload_sigmoid_dfactors(uint32_t map_steps, std::string &err)
+{
+    if (rw.rho.size() < 8)
+    {
+        err = "RHO_TYPE sigmoid needs 8 RHO values {K1, A1, eps1, B1, K2, A2, eps2, B2}";
+        return false;
+    }
+    if (img.n_phases != 1)
+    {
+        err = "RHO_TYPE sigmoid needs a single-phase image";
+        return false;
+    }
+    std::vector<double> f(collisions.size());
+    for (size_t i = 0; i < f.size(); i++)
+    {
+        // updateXIrate (walker.h:162-172, LOG_XIRATE false) -> setSurfaceRelaxivity -> computeDecreaseFactor
+        const double xi = (double)collisions[i] / (double)map_steps;
+        f[i] = decrease_factor(sigmoid_rho(xi));
+    }
+    if (rwnmr_walkers_set_dfactor(ctx, f.data()) != RWNMR_OK)
+    {
+        err = std::string("per-walker decrease factors: ") + rwnmr_last_error(ctx);
+        return false;
+    }
+    walker_dfactors = f;
+    return true;
+}
+
 std::vector<double> Simulation::phase_dfactors() const
 {
     std::vector<double> f(rho_phase.size());
@@ -358,11 +395,9 @@ bool CpmgSequence::set(std::string &err)
     const bool need_map = sim.rw.rho_type == "sigmoid" || cfg.method == "histogram" ||
                           (cfg.save_mode && (cfg.save_histogram || cfg.save_histogram_list || cfg.save_walkers));
     if (need_map && !sim.map_simulation(err)) return false;
-    if (sim.rw.rho_type == "sigmoid" && cfg.method != "histogram")
-    {
-        err = "RHO_TYPE sigmoid (a relaxivity per walker) runs with METHOD: histogram in this build";
+    // updateWalkersRelaxativity(sigmoid) (NMR_cpmg.cpp:137-146): a decrease factor per walker
+    if (sim.rw.rho_type == "sigmoid" && cfg.method != "histogram" && !sim.upload_sigmoid_dfactors(sim.steps, err))
         return false;
-    }
     return true;
 }
 
@@ -378,13 +413,7 @@ bool CpmgSequence::run_simulation(std::string &err)
         {
             const double xi = sim.histogram.bins[k];
             double rho = sim.rho_phase[0];
-            if (sim.rw.rho_type == "sigmoid" && sim.rw.rho.size() >= 8)
-            {
-                const std::vector<double> &p = sim.rw.rho;
-                const double s1 = p[1] + ((p[0] - p[1]) / (1 + std::exp((-1) * p[3] * (xi - p[2]))));
-                const double s2 = p[5] + ((p[4] - p[5]) / (1 + std::exp((-1) * p[7] * (xi - p[6]))));
-                rho = s1 + s2;
-            }
+            if (sim.rw.rho_type == "sigmoid" && sim.rw.rho.size() >= 8) rho = sim.sigmoid_rho(xi);
             pen[k] = std::pow(sim.decrease_factor(rho), xi * (double)sim.rw.steps_per_echo);
         }
         amps.assign(1, 1.0);
@@ -402,6 +431,60 @@ bool CpmgSequence::run_simulation(std::string &err)
         }
         raw = amps;
     }
+    else if (cfg.residual_field != "none")
+    {
+        // RESIDUAL_FIELD (NMR_cpmg.cpp:48-64): the reference applies the field in its GPU walk
+        // (CPMG_walk_*_field, NMR_cpmg_cuda.cpp:1008-1012, 1184-1258); its OpenMP walk ignores it.
+        rwnmr_status st;
+        if (cfg.residual_field == "uniform")
+            st = rwnmr_field_set_uniform(sim.ctx, cfg.gradient_value, cfg.gradient_direction, sim.resolution);
+        else
+        {
+            // InternalField::readDataFromFile: raw doubles, x fastest, exactly one per voxel
+            const int64_t vol = (int64_t)sim.img.nx * sim.img.ny * sim.img.nz;
+            std::ifstream in(cfg.path_to_field, std::ios::binary | std::ios::ate);
+            if (!in)
+            {
+                err = "cannot open internal field file " + cfg.path_to_field;
+                return false;
+            }
+            const int64_t bytes = (int64_t)in.tellg();
+            if (bytes / (int64_t)sizeof(double) != vol)
+            {
+                err = "internal field dims don't match the image: " + std::to_string(bytes / (int64_t)sizeof(double)) +
+                      " vs. " + std::to_string(vol);
+                return false;
+            }
+            std::vector<double> field((size_t)vol);
+            in.seekg(0);
+            in.read(reinterpret_cast<char *>(field.data()), vol * (int64_t)sizeof(double));
+            if (!in)
+            {
+                err = "error reading internal field file " + cfg.path_to_field;
+                return false;
+            }
+            st = rwnmr_field_upload(sim.ctx, field.data(), vol);
+        }
+        std::vector<double> f = sim.phase_dfactors();
+        rwnmr_field_cpmg_params p{};
+        p.bc = sim.bc_code();
+        p.shift = sim.shift;
+        p.steps_per_echo = sim.rw.steps_per_echo;
+        p.n_echoes = (int32_t)E;
+        p.dfactor = sim.rw.rho_type == "sigmoid" ? nullptr : f.data(); // NULL: per-walker factors
+        p.gamma = 1.0e+06 * sim.gamma;   // image_simulation_cuda: gamma = 1e6 * giromagneticRatio
+        p.time_interval = 1.0e-3 * sim.dt; // timeInterval = 1e-3 * NMR.getTimeInterval()
+        raw.assign(E + 1, 0.0);
+        echo_collisions.assign((size_t)E * sim.img.n_phases, 0); // the field walk records no collisions per echo
+        if (st == RWNMR_OK) st = rwnmr_cpmg_field_run(sim.ctx, &p, raw.data(), nullptr);
+        if (st != RWNMR_OK)
+        {
+            err = std::string("CPMG field walk: ") + rwnmr_last_error(sim.ctx);
+            return false;
+        }
+        kernel_ms = rwnmr_ctx_last_kernel_ms(sim.ctx);
+        amps = raw;
+    }
     else
     {
         std::vector<double> f = sim.phase_dfactors();
@@ -410,7 +493,7 @@ bool CpmgSequence::run_simulation(std::string &err)
         p.shift = sim.shift;
         p.steps_per_echo = sim.rw.steps_per_echo;
         p.n_echoes = (int32_t)E;
-        p.dfactor = f.data();
+        p.dfactor = sim.rw.rho_type == "sigmoid" ? nullptr : f.data(); // NULL: per-walker factors
         raw.assign(E + 1, 0.0);
         echo_collisions.assign((size_t)E * sim.img.n_phases, 0);
         rwnmr_status st = rwnmr_cpmg_run(sim.ctx, &p, raw.data(), nullptr, echo_collisions.data());
@@ -573,8 +656,16 @@ bool PfgseSequence::run(std::string &err)
     }
     if (S.rw.rho_type == "sigmoid")
     {
-        err = "RHO_TYPE sigmoid (a relaxivity per walker) is not available for PFGSE in this build";
-        return false;
+        // runInitialMapSimulation (NMR_pfgse.cpp:322-346): a mapping walk as long as the longest
+        // exposure time sets each walker's collision rate, hence its relaxivity
+        const uint32_t map_steps = steps[nd - 1];
+        S.collisions.assign(S.x0.size(), 0);
+        if (rwnmr_map_run(S.ctx, S.bc_code(), S.shift, map_steps, S.collisions.data()) != RWNMR_OK)
+        {
+            err = std::string("collision mapping: ") + rwnmr_last_error(S.ctx);
+            return false;
+        }
+        if (!S.upload_sigmoid_dfactors(map_steps, err)) return false;
     }
     // one GPU call walks all exposure times cumulatively (the reference GPU path's stepsTaken)
     std::vector<double> f = S.phase_dfactors();
@@ -587,7 +678,7 @@ bool PfgseSequence::run(std::string &err)
     p.n_g = n_g;
     p.kvec = kvec.data();
     p.res = S.voxel_res;
-    p.dfactor = f.data();
+    p.dfactor = S.rw.rho_type == "sigmoid" ? nullptr : f.data(); // NULL: per-walker factors
     Mkt.assign((size_t)nd * n_g, 0.0);
     esum.assign(nd, 0.0);
     std::vector<uint64_t> msd((size_t)nd * 3);

@@ -58,6 +58,7 @@ class Simulation
     uint32_t steps = 0, echoes = 0;
     std::vector<uint32_t> collisions;
     std::vector<double> xi_rate;
+    std::vector<double> walker_dfactors; // RHO_TYPE sigmoid: the factors last uploaded
     Histogram histogram;
     std::vector<Histogram> hist_list;
     rwnmr_ctx *ctx = nullptr;
@@ -77,6 +78,10 @@ class Simulation
     // collision-mapping walk with histogram windows (mapSimulation, NMR_Simulation.cpp:1787-1841)
     bool map_simulation(std::string &err);
     double decrease_factor(double rho) const; // Walker::computeDecreaseFactor
+    double sigmoid_rho(double xi) const;      // Walker::setSurfaceRelaxivity(vector) at collision rate xi
+    // per-walker decrease factors from the sigmoid of each walker's collision rate over `steps`
+    // steps of the last mapping walk (NMR_Simulation::updateWalkersRelaxativity)
+    bool upload_sigmoid_dfactors(uint32_t steps, std::string &err);
     std::vector<double> phase_dfactors() const;
     int bc_code() const;
     void save_info() const;

@@ -39,6 +39,13 @@ struct DevImage
     int32_t shift;
 };
 
+// 64-bit words per bit-block for NP phase slots (1, 2 or 4).
+template <int NP>
+struct WordsPerBlock
+{
+    static constexpr int value = NP == 1 ? 1 : (NP == 2 ? 2 : 4);
+};
+
 __device__ __forceinline__ uint64_t xorshift64(uint64_t x)
 {
     x ^= x << 13;
@@ -111,6 +118,56 @@ __device__ __forceinline__ void init_image_coords(const DevImage &im, WalkerPos 
         p.iy = p.y;
         p.iz = p.z;
     }
+}
+
+// Image voxel of the walker's current position: pos >> shift (noflux), the periodic / mirrored
+// image index otherwise (NMR_cpmg_cuda.cpp:1986-2015).
+template <int BC>
+__device__ __forceinline__ void current_voxel(const DevImage &im, const WalkerPos &p, int &ix, int &iy, int &iz)
+{
+    if (BC == BC_NOFLUX)
+    {
+        ix = p.x;
+        iy = p.y;
+        iz = p.z;
+    }
+    else if (BC == BC_PERIODIC || BC == BC_MIRROR)
+    {
+        ix = p.ix;
+        iy = p.iy;
+        iz = p.iz;
+    }
+    else
+    {
+        const int s = im.shift;
+        if (im.bc == BC_PERIODIC)
+        {
+            ix = map_periodic(p.x, s, im.nx);
+            iy = map_periodic(p.y, s, im.ny);
+            iz = map_periodic(p.z, s, im.nz);
+        }
+        else if (im.bc == BC_MIRROR)
+        {
+            ix = map_mirror(p.x, s, im.nx);
+            iy = map_mirror(p.y, s, im.ny);
+            iz = map_mirror(p.z, s, im.nz);
+        }
+        else
+        {
+            ix = p.x >> s;
+            iy = p.y >> s;
+            iz = p.z >> s;
+        }
+    }
+}
+
+// Solid bit of an image voxel (word 0 of its block).
+template <int W>
+__device__ __forceinline__ bool voxel_solid(const DevImage &im, int ix, int iy, int iz)
+{
+    const int64_t blk = (int64_t)(ix >> 2) + (int64_t)(iy >> 2) * im.bcols + (int64_t)(iz >> 2) * im.bcr;
+    const uint32_t bit = (uint32_t)((ix & 3) | ((iy & 3) << 2) | ((iz & 3) << 4));
+    return ((__ldg(im.blocks + blk * W) >> bit) & 1ull) != 0;
 }
 
 // Returns true if a walker may start at p: inside the image for noflux (in walk units).

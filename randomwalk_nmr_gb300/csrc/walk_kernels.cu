@@ -30,11 +30,8 @@ namespace
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint64_t M21 = (1ull << 21) - 1;
 
-template <int NP>
-struct WordsPerBlock
-{
-    static constexpr int value = NP == 1 ? 1 : (NP == 2 ? 2 : 4);
-};
+// 2^63 fixed point of an energy in [0, 1]: round(e * 2^63), the rounding of the energy tables.
+__device__ __forceinline__ uint64_t walker_fx(double e) { return __double2ull_rn(e * 0x1p63); }
 
 __device__ __forceinline__ void load_pos(const WalkState &s, int64_t i, WalkerPos &p, uint64_t &seed)
 {
@@ -49,11 +46,22 @@ __device__ __forceinline__ void load_pos(const WalkState &s, int64_t i, WalkerPo
 // CPMG / collision-mapping walk over echoes [e_begin, e_end).
 // acc layout: [(n_echoes+1)][K], K = 3 + NP: limbs of the energy sum after echo e (index e+1;
 // index 0 = initial state) and, for k = 3 + p, collisions on phase p gained during echo e.
-template <int BC, int NP>
+// PACK (two phases; at most 2047 steps per recorded echo, 65535 per unrecorded one): a lane
+// counts both phases' collisions of the echo in the 16-bit halves of one word, and one
+// redux.sync sums both halves over the warp (at most 32 * 2047 < 2^16 each).
+// WF (single phase): every walker has its own decrease factor f_w (the reference's per-walker
+// Walker::decreaseFactor, e.g. from a sigmoid of its collision rate) and its energy is the FP64
+// repeated product f_w * f_w * ..., one multiply per collision as in Walker::walk_3D, applied after
+// each echo for the collisions the echo gained and rounded to the same 2^63 fixed point.
+template <int BC, int NP, bool PACK, bool WF>
 __global__ void __launch_bounds__(kWalkThreads) cpmg_walk_kernel(DevImage im, WalkState st, CpmgLaunch L)
 {
+    static_assert(!PACK || NP == 2, "packed collision counts are for two phases");
+    static_assert(!WF || NP == 1, "per-walker decrease factors are for single-phase images");
     constexpr int W = WordsPerBlock<NP>::value;
-    constexpr int K = 3 + NP;
+    constexpr int NG = PACK ? 1 : NP; // collision-count words per echo
+    constexpr int KK = 3 + NG;        // values kept per echo
+    constexpr int K = 3 + NP;         // values per echo in the accumulators
     __shared__ unsigned long long sacc[32 * K];
 
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -88,15 +96,23 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_walk_kernel(DevImage im, Wa
         init_image_coords<BC>(im, p);
     }
 
+    double fw = 1.0, ew = 1.0; // WF: decrease factor and energy of this walker
+    if (WF && active)
+    {
+        fw = L.wf[i];
+        ew = L.from_initial ? 1.0 : L.wenergy[i];
+    }
+
     for (int k = threadIdx.x; k < 32 * K; k += blockDim.x) sacc[k] = 0;
 
-    uint64_t efx = (active && L.record) ? energy_fx<NP>(L.tfx, L.tstride, c) : 0;
+    uint64_t efx = 0;
+    if (active && L.record) efx = WF ? walker_fx(ew) : energy_fx<NP>(L.tfx, L.tstride, c);
     if (L.record && L.e_begin == 0)
     {
         // initial energy sum (output index 0)
-        uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
-        uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((efx >> 21) & M21));
-        uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
+        const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
+        const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((efx >> 21) & M21));
+        const uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
         if (lane == 0)
         {
             atomicAdd(&L.acc[0], (unsigned long long)r0);
@@ -109,14 +125,14 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_walk_kernel(DevImage im, Wa
     for (int e0 = L.e_begin; e0 < L.e_end; e0 += 32)
     {
         const int e1 = min(e0 + 32, L.e_end);
-        uint32_t keep[K];
+        uint32_t keep[KK];
 #pragma unroll
-        for (int k = 0; k < K; k++) keep[k] = 0;
+        for (int k = 0; k < KK; k++) keep[k] = 0;
         for (int e = e0; e < e1; e++)
         {
-            uint32_t gained[NP];
+            uint32_t g[NG]; // collisions gained this echo, per phase (PACK: 16 bits per phase)
 #pragma unroll
-            for (int q = 0; q < NP; q++) gained[q] = 0;
+            for (int k = 0; k < NG; k++) g[k] = 0;
             if (active)
             {
                 for (int s = 0; s < L.steps_per_echo; s++)
@@ -124,32 +140,56 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_walk_kernel(DevImage im, Wa
                     bool wall;
                     int ph;
                     walker_step<BC, W>(im, p, seed, wall, ph);
+                    if (PACK) g[0] += (wall ? 1u : 0u) << (ph << 4);
+                    else
+                    {
 #pragma unroll
-                    for (int q = 0; q < NP; q++) gained[q] += (wall && ph == q) ? 1u : 0u;
+                        for (int q = 0; q < NP; q++) g[q] += (wall && ph == q) ? 1u : 0u;
+                    }
                 }
                 bool changed = false;
-#pragma unroll
-                for (int q = 0; q < NP; q++)
+                if (PACK)
                 {
-                    c[q] += gained[q];
-                    changed |= gained[q] != 0;
+                    c[0] += g[0] & 0xffffu;
+                    c[1] += g[0] >> 16;
+                    changed = g[0] != 0;
                 }
-                if (changed && L.record) efx = energy_fx<NP>(L.tfx, L.tstride, c);
+                else
+                {
+#pragma unroll
+                    for (int q = 0; q < NP; q++)
+                    {
+                        c[q] += g[q];
+                        changed |= g[q] != 0;
+                    }
+                }
+                if (changed && L.record)
+                {
+                    if (WF)
+                    {
+                        for (uint32_t k = 0; k < g[0]; k++) ew = ew * fw;
+                        efx = walker_fx(ew);
+                    }
+                    else
+                    {
+                        efx = energy_fx<NP>(L.tfx, L.tstride, c);
+                    }
+                }
             }
             if (L.record)
             {
-                uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
-                uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((efx >> 21) & M21));
-                uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
+                const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
+                const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((efx >> 21) & M21));
+                const uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
                 const bool mine = lane == (e - e0);
                 keep[0] = mine ? r0 : keep[0];
                 keep[1] = mine ? r1 : keep[1];
                 keep[2] = mine ? r2 : keep[2];
 #pragma unroll
-                for (int q = 0; q < NP; q++)
+                for (int k = 0; k < NG; k++)
                 {
-                    uint32_t rq = __reduce_add_sync(FULL, gained[q]);
-                    keep[3 + q] = mine ? rq : keep[3 + q];
+                    const uint32_t rg = __reduce_add_sync(FULL, g[k]);
+                    keep[3 + k] = mine ? rg : keep[3 + k];
                 }
             }
         }
@@ -158,9 +198,16 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_walk_kernel(DevImage im, Wa
             // lane l holds this warp's sums for echo e0 + l
             if (lane < e1 - e0)
             {
+                unsigned long long *sa = &sacc[lane * K];
 #pragma unroll
-                for (int k = 0; k < K; k++)
-                    if (keep[k]) atomicAdd(&sacc[lane * K + k], (unsigned long long)keep[k]);
+                for (int k = 0; k < 3; k++)
+                    if (keep[k]) atomicAdd(&sa[k], (unsigned long long)keep[k]);
+#pragma unroll
+                for (int q = 0; q < NP; q++)
+                {
+                    const uint32_t v = PACK ? (keep[3] >> (16 * q)) & 0xffffu : keep[3 + q];
+                    if (v) atomicAdd(&sa[3 + q], (unsigned long long)v);
+                }
             }
             __syncthreads();
             for (int k = threadIdx.x; k < (e1 - e0) * K; k += blockDim.x)
@@ -181,6 +228,7 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_walk_kernel(DevImage im, Wa
         st.seed[i] = seed;
 #pragma unroll
         for (int q = 0; q < NP; q++) st.coll[(size_t)q * st.n + i] = c[q];
+        if (WF) L.wenergy[i] = ew;
     }
 }
 
@@ -283,9 +331,11 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_adjoint_kernel(DevImage im,
 //     one per walker (pfgse_phase_kernel);
 //   * for any other gradient direction, each walker's displacement and FP64 energy, measured by
 //     pfgse_direct_kernel.
-template <int BC, int NP>
+// WF: per-walker decrease factors, energies as FP64 repeated products (see cpmg_walk_kernel).
+template <int BC, int NP, bool WF>
 __global__ void __launch_bounds__(kWalkThreads) pfgse_walk_kernel(DevImage im, WalkState st, PfgseLaunch L)
 {
+    static_assert(!WF || NP == 1, "per-walker decrease factors are for single-phase images");
     constexpr int W = WordsPerBlock<NP>::value;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -312,6 +362,9 @@ __global__ void __launch_bounds__(kWalkThreads) pfgse_walk_kernel(DevImage im, W
         }
         init_image_coords<BC>(im, p);
     }
+    const double fw = (WF && active) ? L.wf[i] : 1.0;
+    double ew = 1.0;
+    uint32_t c_done = 0; // WF: collisions already folded into ew
     int done = 0;
     for (int d = 0; d < L.n_delta; d++)
     {
@@ -327,7 +380,12 @@ __global__ void __launch_bounds__(kWalkThreads) pfgse_walk_kernel(DevImage im, W
                 for (int q = 0; q < NP; q++) c[q] += (wall && ph == q) ? 1u : 0u;
             }
         }
-        const uint64_t efx = active ? energy_fx<NP>(L.tfx, L.tstride, c) : 0ull;
+        if (WF)
+        {
+            for (; c_done < c[0]; c_done++) ew = ew * fw;
+        }
+        uint64_t efx = 0;
+        if (active) efx = WF ? walker_fx(ew) : energy_fx<NP>(L.tfx, L.tstride, c);
         const int ddx = p.x - x0, ddy = p.y - y0, ddz = p.z - z0;
         unsigned long long *acc = L.acc + (size_t)d * 6;
         uint32_t r;
@@ -370,7 +428,7 @@ __global__ void __launch_bounds__(kWalkThreads) pfgse_walk_kernel(DevImage im, W
                 L.disp[o * 3 + 0] = ddx;
                 L.disp[o * 3 + 1] = ddy;
                 L.disp[o * 3 + 2] = ddz;
-                L.energy[o] = energy_fp64<NP>(L.t, L.tstride, c);
+                L.energy[o] = WF ? ew : energy_fp64<NP>(L.t, L.tstride, c);
             }
         }
     }
@@ -535,7 +593,19 @@ cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkS
         constexpr int NP = decltype(npc)::value;
         with_bc<NP>(bc_key, [&](auto bcc) {
             constexpr int BC = decltype(bcc)::value;
-            cpmg_walk_kernel<BC, NP><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            // packed counts: a lane's half-word holds at most steps_per_echo < 2^16 collisions, and a
+            // recorded echo's warp sum of a half at most 32 * steps_per_echo < 2^16
+            if constexpr (NP == 1)
+            {
+                if (L.wf)
+                    cpmg_walk_kernel<BC, 1, false, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                else
+                    cpmg_walk_kernel<BC, 1, false, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            }
+            else if (NP == 2 && L.steps_per_echo <= (L.record ? 2047 : 65535))
+                cpmg_walk_kernel<BC, NP, NP == 2, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            else
+                cpmg_walk_kernel<BC, NP, false, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
         });
     };
     if (np == 1) go(std::integral_constant<int, 1>{});
@@ -567,7 +637,15 @@ cudaError_t launch_pfgse_walk(int bc_key, int np, const DevImage &im, const Walk
         constexpr int NP = decltype(npc)::value;
         with_bc<NP>(bc_key, [&](auto bcc) {
             constexpr int BC = decltype(bcc)::value;
-            pfgse_walk_kernel<BC, NP><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            if constexpr (NP == 1)
+            {
+                if (L.wf)
+                    pfgse_walk_kernel<BC, 1, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                else
+                    pfgse_walk_kernel<BC, 1, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            }
+            else
+                pfgse_walk_kernel<BC, NP, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
         });
     };
     if (np == 1) go(std::integral_constant<int, 1>{});

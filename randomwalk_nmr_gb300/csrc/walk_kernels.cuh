@@ -37,7 +37,27 @@ struct CpmgLaunch
     int record;            // accumulate per-echo sums into acc
     const uint64_t *tfx;   // [n_phases][tstride] fixed-point energy tables
     int tstride;
+    const double *wf;      // per-walker decrease factors [n] (single phase), or null for the tables
+    double *wenergy;       // per-walker FP64 energies [n], carried across launches (with wf)
     unsigned long long *acc; // [(n_echoes+1)][3 + NP]
+    unsigned *status;
+};
+
+struct FieldLaunch
+{
+    int e_begin, e_end;      // echoes walked by this launch
+    int steps_per_inversion; // steps_per_echo / 2
+    int from_initial;        // 1: start from (x0, seed0), no collisions, phase 0; 0: continue
+    const double *t;         // [n_phases][tstride] FP64 survival tables
+    int tstride;
+    double gammatau;         // 0.5 * gamma * time interval
+    const double *field;     // array field [nz][ny][nx]
+    double dg;               // uniform field: value per voxel along `axis` (0 in solid voxels)
+    int axis;
+    double *phase;           // [n] walker phases, carried across launches
+    const double *wf;        // per-walker decrease factors [n] (single phase), or null for the tables
+    double *palive;          // with wf: per-walker survival probabilities [n], carried across launches
+    unsigned long long *acc; // [(n_echoes+1)][3] limbs of sum(round(E * 2^61) + 2^61)
     unsigned *status;
 };
 
@@ -64,6 +84,7 @@ struct PfgseLaunch
     unsigned long long *hist; // [n_delta][2*hist_half+1][2]
     int32_t *disp;            // general path: [n_delta][n][3]
     double *energy;           // general path: [n_delta][n]
+    const double *wf;         // per-walker decrease factors [n] (single phase), or null for the tables
     unsigned *status;
 };
 
@@ -95,6 +116,8 @@ struct DirectLaunch
 
 cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkState &st, const CpmgLaunch &L,
                              dim3 grid, cudaStream_t s);
+cudaError_t launch_cpmg_field(int bc_key, int np, bool uniform, const DevImage &im, const WalkState &st,
+                              const FieldLaunch &L, dim3 grid, cudaStream_t s);
 cudaError_t launch_cpmg_adjoint(int bc_key, int np, const DevImage &im, const WalkState &st, const AdjointLaunch &L,
                                 dim3 grid, cudaStream_t s);
 cudaError_t launch_pfgse_walk(int bc_key, int np, const DevImage &im, const WalkState &st, const PfgseLaunch &L,

@@ -37,7 +37,8 @@ EXPORTS = [
     "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_map_continue", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
     "rwnmr_cpmg_run_noalloc", "rwnmr_batch_create", "rwnmr_batch_destroy", "rwnmr_batch_last_error",
     "rwnmr_batch_last_kernel_ms", "rwnmr_batch_launch_count", "rwnmr_batch_add_image", "rwnmr_batch_cpmg",
-    "rwnmr_batch_autotune",
+    "rwnmr_batch_autotune", "rwnmr_field_set_uniform", "rwnmr_field_upload", "rwnmr_field_clear",
+    "rwnmr_cpmg_field_run", "rwnmr_walkers_set_dfactor",
 ]
 
 
@@ -52,6 +53,14 @@ class CpmgParams(ctypes.Structure):
         ("bc", ctypes.c_int32), ("shift", ctypes.c_int32), ("steps_per_echo", ctypes.c_int32),
         ("n_echoes", ctypes.c_int32), ("dfactor", ctypes.POINTER(ctypes.c_double)),
         ("echoes_per_launch", ctypes.c_int32),
+    ]
+
+
+class FieldCpmgParams(ctypes.Structure):
+    _fields_ = [
+        ("bc", ctypes.c_int32), ("shift", ctypes.c_int32), ("steps_per_echo", ctypes.c_int32),
+        ("n_echoes", ctypes.c_int32), ("dfactor", ctypes.POINTER(ctypes.c_double)), ("gamma", ctypes.c_double),
+        ("time_interval", ctypes.c_double), ("echoes_per_launch", ctypes.c_int32),
     ]
 
 
@@ -106,6 +115,8 @@ def _p(a):
 
 
 def _dptr(a):
+    if a is None:
+        return ctypes.POINTER(ctypes.c_double)()
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
@@ -193,7 +204,16 @@ class Engine:
         self._check(self.lib.rwnmr_walkers_download(self.ctx, _p(x), _p(y), _p(z), _p(s), _p(c)))
         return dict(x=x, y=y, z=z, seed=s, collisions=c)
 
+    def set_walker_dfactor(self, dfactor):
+        """Per-walker decrease factors (single-phase images); walks called with dfactor=None use them."""
+        f = np.ascontiguousarray(dfactor, np.float64)
+        if f.shape != (self.n,):
+            raise ValueError("one decrease factor per walker")
+        self._check(self.lib.rwnmr_walkers_set_dfactor(self.ctx, _p(f)))
+
     def _dfactor(self, dfactor):
+        if dfactor is None:
+            return None
         return np.ascontiguousarray(np.broadcast_to(np.asarray(dfactor, np.float64), (self.n_phases,)))
 
     # -- walks ------------------------------------------------------------------------------
@@ -217,6 +237,31 @@ class Engine:
         out = np.zeros(self.n_phases)
         self._check(self.lib.rwnmr_cpmg_adjoint(self.ctx, ctypes.byref(prm), _p(g), _p(out)))
         return out
+
+    # -- internal field ---------------------------------------------------------------------
+    def set_field_uniform(self, gradient: float, direction: int, resolution: float):
+        """RESIDUAL_FIELD: uniform -- B = coord * gradient * 1e-6 * resolution in pores, 0 in solid."""
+        self._check(self.lib.rwnmr_field_set_uniform(self.ctx, ctypes.c_double(gradient), int(direction),
+                                                     ctypes.c_double(resolution)))
+
+    def upload_field(self, values: np.ndarray):
+        """RESIDUAL_FIELD: import -- one value per image voxel, shape (nz, ny, nx)."""
+        v = np.ascontiguousarray(values, np.float64)
+        self._check(self.lib.rwnmr_field_upload(self.ctx, _p(v), ctypes.c_int64(v.size)))
+
+    def clear_field(self):
+        self._check(self.lib.rwnmr_field_clear(self.ctx))
+
+    def cpmg_field(self, n_echoes: int, steps_per_echo: int, dfactor, gamma: float, time_interval: float,
+                   bc: str = "noflux", shift: int = 0, echoes_per_launch: int = 0):
+        """CPMG walk in the internal field; returns the echo energy sums and final walker phases."""
+        df = self._dfactor(dfactor)
+        prm = FieldCpmgParams(BC[bc], int(shift), int(steps_per_echo), int(n_echoes), _dptr(df), float(gamma),
+                              float(time_interval), int(echoes_per_launch))
+        echo_sum = np.zeros(n_echoes + 1)
+        phase = np.zeros(self.n)
+        self._check(self.lib.rwnmr_cpmg_field_run(self.ctx, ctypes.byref(prm), _p(echo_sum), _p(phase)))
+        return dict(echo_sum=echo_sum, phase=phase)
 
     def map(self, steps: int, bc: str = "noflux", shift: int = 0) -> np.ndarray:
         out = np.zeros(self.n, np.uint32)

@@ -68,6 +68,23 @@ def main():
                pfgse_steps=pf["steps"], pfgse_dsat=pf["dsat"], pfgse_dmsd=pf["dmsd"], pfgse_kvec=pf["kvec"],
                pfgse_delta=pf["delta"], pfgse_gamma=np.array(rs3.info["gamma"]))
 
+    # RHO_TYPE sigmoid: every walker's relaxivity from its collision rate in the mapping walk
+    # (NMR_cpmg.cpp:132-146, Walker/walker.h:162-196), image-based CPMG and PFGSE
+    sig = (40.0, 5.0, 0.1, 30.0, 10.0, 0.0, 0.25, 50.0)
+    out["sigmoid_rho"] = np.array(sig)
+    rs4 = RefSim(lab, 400, 5, rho=sig, rho_type="sigmoid", steps_per_echo=3, bulk_time=800.0)
+    c = rs4.cpmg(obs_time=12.0, apply_bulk=True)
+    x, y, z, s, df = rs4.walkers()
+    out.update(cpmg_sig_raw=c["raw"], cpmg_sig_signal=c["signal"], cpmg_sig_dfactor=df,
+               cpmg_sig_map_collisions=c["map_collisions"])
+    del rs4
+    rs5 = RefSim(lab, 500, 9, rho=sig, rho_type="sigmoid", steps_per_echo=1)
+    pf = rs5.pfgse(pulse_width=0.5, gmax=(0.0, 0.0, 400.0), n_g=8, time_seq="manual", n_t=3,
+                   t_values=[0.4, 1.0, 2.5], threshold_type="samples", threshold_value=8)
+    x, y, z, s, df = rs5.walkers()
+    out.update(pfgse_sig_Mkt=pf["Mkt"], pfgse_sig_dsat=pf["dsat"], pfgse_sig_dmsd=pf["dmsd"], pfgse_sig_dfactor=df)
+    del rs5
+
     # walker placement modes (no one-past-the-end pore draws in these cases)
     lab_p = lab.copy()
     nz, ny, nx = lab_p.shape

@@ -44,6 +44,69 @@ def test_cli_cpmg_matches_reference_sequence(tmp_path, golden):
     assert os.path.exists(str(tmp_path / "db" / "t" / "SimInfo.txt"))
 
 
+def test_cli_cpmg_internal_field(tmp_path, golden, oracle):
+    """RESIDUAL_FIELD uniform / import through the config files: a zero field reproduces the
+    plain decay, an imported copy of the uniform field reproduces the uniform run, a field file
+    of the wrong size is rejected."""
+    def run(name, extra):
+        root = str(tmp_path / name / "config") + "/"
+        write(root + "default/rwnmr.config", RW.format(bulk=800.0, rho=25.0, n=400, spe=4, seed=5))
+        write(root + "default/uct.config", "RESOLUTION: 1.0\nVOXEL_DIVISION: 0\n")
+        write(root + "default/cpmg.config", "METHOD: image-based\nOBS_TIME: 6.0\nAPPLY_BULK: true\nSAVE_MODE: true\n"
+                                            "SAVE_DECAY: true\n" + extra)
+        rc = host.cli(["--config-root", root, "--synthetic", IMG_A, "--quiet", "cpmg"], cwd=str(tmp_path / name))
+        if rc != 0:
+            return None
+        d = str(tmp_path / name / "db" / "t") + "//NMR_cpmg_t=6.00ms"
+        return np.loadtxt(d + "/cpmg_decay.csv", delimiter=",", skiprows=1)
+
+    plain = run("plain", "")
+    zero = run("zero", "RESIDUAL_FIELD: uniform\nGRADIENT_VALUE: 0.0\nGRADIENT_DIRECTION: z\n")
+    np.testing.assert_allclose(zero[:, 1], plain[:, 1], rtol=1e-14)
+    uni = run("uni", "RESIDUAL_FIELD: uniform\nGRADIENT_VALUE: 8.0\nGRADIENT_DIRECTION: y\n")
+    assert uni[-1, 1] < 0.98 * plain[-1, 1]
+    field = oracle.uniform_field(golden["img_a"], 1.0, 8.0, 1)
+    path = str(tmp_path / "field.raw")
+    field.tofile(path)
+    imp = run("imp", f"RESIDUAL_FIELD: import\nPATH_TO_FIELD: {path}\n")
+    assert np.array_equal(imp, uni)
+    field[:-1].tofile(path)
+    assert run("bad", f"RESIDUAL_FIELD: import\nPATH_TO_FIELD: {path}\n") is None
+
+
+def test_cli_sigmoid_relaxivity_matches_reference(tmp_path, golden):
+    """RHO_TYPE sigmoid: a relaxivity per walker from its collision rate in the mapping walk, for
+    image-based CPMG and for PFGSE, against the reference's own CPU sequences."""
+    sig = ", ".join(repr(float(v)) for v in golden["sigmoid_rho"])
+    rw_sig = RW.replace("RHO_TYPE: uniform", "RHO_TYPE: sigmoid")
+    root = str(tmp_path / "c" / "config") + "/"
+    write(root + "default/rwnmr.config", rw_sig.format(bulk=800.0, rho=sig, n=400, spe=3, seed=5))
+    write(root + "default/uct.config", "RESOLUTION: 1.0\nVOXEL_DIVISION: 0\n")
+    write(root + "default/cpmg.config", "METHOD: image-based\nOBS_TIME: 12.0\nAPPLY_BULK: true\nSAVE_MODE: true\n"
+                                        "SAVE_DECAY: true\n")
+    assert host.cli(["--config-root", root, "--synthetic", IMG_A, "--quiet", "cpmg"], cwd=str(tmp_path / "c")) == 0
+    d = str(tmp_path / "c" / "db" / "t") + "//NMR_cpmg_t=12.00ms"
+    decay = np.loadtxt(d + "/cpmg_decay.csv", delimiter=",", skiprows=1)
+    np.testing.assert_allclose(decay[:, 1], golden["cpmg_sig_signal"], rtol=1e-12)
+
+    root = str(tmp_path / "p" / "config") + "/"
+    write(root + "default/rwnmr.config", rw_sig.format(bulk=2800.0, rho=sig, n=500, spe=1, seed=9))
+    write(root + "default/uct.config", "RESOLUTION: 1.0\nVOXEL_DIVISION: 0\n")
+    write(root + "default/pfgse.config",
+          "APPLY_BULK: false\nPULSE_WIDTH: 0.5\nMAX_GRADIENT: {0.0, 0.0, 400.0}\nGRADIENT_SAMPLES: 8\n"
+          "TIME_SEQ: manual\nTIME_SAMPLES: 3\nTIME_VALUES: {0.4, 1.0, 2.5}\nAPPLY_SCALE_FACTOR: false\n"
+          "THRESHOLD_TYPE: samples\nTHRESHOLD_VALUE: 8\nALLOW_WALKER_SAMPLING: false\nSAVE_MODE: true\n"
+          "SAVE_PFGSE: true\n")
+    assert host.cli(["--config-root", root, "--synthetic", IMG_A, "--quiet", "pfgse"], cwd=str(tmp_path / "p")) == 0
+    d = str(tmp_path / "p" / "db" / "t") + "//NMR_pfgse"
+    res = np.loadtxt(d + "/PFGSE_results.csv", delimiter=",", skiprows=1, ndmin=2)
+    np.testing.assert_allclose(res[:, 1], golden["pfgse_sig_dsat"], rtol=1e-10)
+    np.testing.assert_allclose(res[:, 5], golden["pfgse_sig_dmsd"], rtol=1e-12)
+    for i in range(3):
+        e = np.loadtxt(d + f"/timesamples/echoes_{i}.csv", delimiter=",", skiprows=1)
+        assert np.all(np.abs(e[:, 2] / e[0, 2] - golden["pfgse_sig_Mkt"][i]) <= 1e-12)
+
+
 def test_cli_pfgse_matches_reference_sequence(tmp_path, golden):
     root = str(tmp_path / "config") + "/"
     write(root + "default/rwnmr.config", RW.format(bulk=2800.0, rho=5.0, n=500, spe=1, seed=9))

@@ -63,6 +63,17 @@ def test_cpmg_parity_multiphase(engine, oracle, n_phases):
     assert np.all(g["echo_coll"].sum(axis=0) > 0)
 
 
+@pytest.mark.parametrize("spe", [2047, 2048, 3001])
+def test_cpmg_two_phase_long_echoes(engine, oracle, spe):
+    """Two phases count collisions in 16-bit halves of one word up to 2047 steps per echo and in
+    separate words beyond; both sides of the switch agree with the oracle."""
+    lab = image(shape=(20, 18, 22), n_phases=2, seed=13, rmin=1.5, rmax=3.0)
+    w = walkers(lab, 700, 9)
+    g, st, o = run_both(engine, oracle, lab, w, 4, spe, dfactor([3.0, 8.0]), n_phases=2)
+    assert_parity(g, st, o)
+    assert g["echo_coll"].max() > 32 * 256  # warp-wide sums well past 8 bits per phase
+
+
 def test_cpmg_parity_reference_golden(engine, golden):
     """Against the reference's own per-echo walk outputs."""
     gd = golden
@@ -140,15 +151,58 @@ def test_cpmg_rejects_bad_input(engine):
         engine.cpmg(10, 1, 1.5)  # decrease factor outside [0, 1]
 
 
-@pytest.mark.parametrize("bc", ["noflux", "periodic"])
-def test_map_walk_matches_oracle(engine, oracle, bc):
-    lab = image(seed=4)
+@pytest.mark.parametrize("bc,n_phases", [("noflux", 1), ("periodic", 1), ("noflux", 2), ("mirror", 4)])
+def test_map_walk_matches_oracle(engine, oracle, bc, n_phases):
+    lab = image(seed=4, n_phases=n_phases)
     w = walkers(lab, 2500, 8)
-    engine.upload_labels(lab)
+    engine.upload_labels(lab, n_phases)
     engine.upload_walkers(*w)
-    coll = engine.map(20000 + 17, bc=bc)
-    d, oc = oracle.displacements(lab, w, 20000 + 17, bc=bc, threads=4)
-    assert np.array_equal(coll, oc[:, 0])
+    coll = engine.map(20000 + 17, bc=bc)  # two launches of up to 16384 steps
+    d, oc = oracle.displacements(lab, w, 20000 + 17, bc=bc, threads=4, n_phases=n_phases)
+    assert np.array_equal(coll, oc.sum(axis=1))
+    assert np.array_equal(engine.download_walkers()["collisions"], oc)
     st = engine.download_walkers()
     assert np.array_equal(st["x"] - w[0], d[0])
     assert np.array_equal(st["z"] - w[2], d[2])
+
+
+def test_cpmg_per_walker_dfactor_reference_golden(engine, golden):
+    """RHO_TYPE sigmoid: every walker relaxes with its own decrease factor (the reference's, from
+    the sigmoid of its collision rate); the echo sums are the reference's raw signal."""
+    gd = golden
+    engine.upload_labels(gd["img_a"])
+    engine.upload_walkers(gd["cpmg_x0"], gd["cpmg_y0"], gd["cpmg_z0"], gd["cpmg_seed0"])
+    engine.set_walker_dfactor(gd["cpmg_sig_dfactor"])
+    n_echoes = len(gd["cpmg_sig_raw"]) - 1
+    g = engine.cpmg(n_echoes, 3, None)
+    np.testing.assert_allclose(g["echo_sum"], gd["cpmg_sig_raw"], rtol=1e-12)
+    # launch chunks carry each walker's energy exactly
+    g2 = engine.cpmg(n_echoes, 3, None, echoes_per_launch=7)
+    assert np.array_equal(g2["echo_fx"], g["echo_fx"]) and np.array_equal(g2["echo_coll"], g["echo_coll"])
+
+
+def test_cpmg_per_walker_dfactor_equal_factors_match_tables(engine):
+    from randomwalk_nmr_gb300 import RwnmrError
+
+    lab = image(seed=12)
+    w = walkers(lab, 3000, 2)
+    engine.upload_labels(lab)
+    engine.upload_walkers(*w)
+    f = dfactor(17.0)
+    t = engine.cpmg(80, 2, f)
+    engine.set_walker_dfactor(np.full(len(w[0]), f))
+    p = engine.cpmg(80, 2, None)
+    assert np.array_equal(p["echo_fx"], t["echo_fx"])
+    assert np.array_equal(p["echo_coll"], t["echo_coll"])
+    with pytest.raises(RwnmrError):
+        engine.cpmg_adjoint(80, 2, None, np.ones(81))
+    with pytest.raises(RwnmrError):
+        engine.set_walker_dfactor(np.full(len(w[0]), 1.5))
+    engine.upload_walkers(*w)  # new walkers drop the factors
+    with pytest.raises(RwnmrError, match="per-walker"):
+        engine.cpmg(10, 2, None)
+    engine.upload_labels(image(n_phases=2, seed=12), 2)
+    engine.upload_walkers(*w)
+    engine.set_walker_dfactor(np.full(len(w[0]), f))
+    with pytest.raises(RwnmrError, match="single-phase"):
+        engine.cpmg(10, 2, None)

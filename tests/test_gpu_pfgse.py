@@ -86,3 +86,24 @@ def test_pfgse_grad_g_matches_finite_differences(engine, gdir):
     Mm = engine.pfgse(steps, np.outer((gvals - h) * kscale, d), 1.0, f)["M"]
     fd = (Mp - Mm) / (2 * h)
     np.testing.assert_allclose(dM, fd, rtol=1e-5, atol=1e-7 * len(w[0]))
+
+
+def test_pfgse_per_walker_dfactor(engine, golden):
+    """RHO_TYPE sigmoid: the reference's per-walker decrease factors give its attenuations; equal
+    per-walker factors reproduce the per-phase tables on both the axis and the general path."""
+    gd = golden
+    engine.upload_labels(gd["img_a"])
+    engine.upload_walkers(gd["pfgse_x0"], gd["pfgse_y0"], gd["pfgse_z0"], gd["pfgse_seed0"])
+    engine.set_walker_dfactor(gd["pfgse_sig_dfactor"])
+    g = engine.pfgse(gd["pfgse_steps"], gd["pfgse_kvec"], 1.0, None)
+    Mkt = g["M"] / g["esum"][:, None]
+    assert np.all(np.abs(Mkt - gd["pfgse_sig_Mkt"]) <= ATT_TOL)
+    lab, w = setup(engine, seed=6)
+    steps = np.array([20, 90, 300], np.int32)
+    f = dfactor(12.0)
+    engine.set_walker_dfactor(np.full(len(w[0]), f))
+    for gdir in ((0, 0, 90.0), (30.0, 40.0, 20.0)):
+        kv = kvecs(8, gdir)
+        a = engine.pfgse(steps, kv, 1.0, f)
+        b = engine.pfgse(steps, kv, 1.0, None)
+        assert np.array_equal(a["esum"], b["esum"]) and np.array_equal(a["M"], b["M"])
