@@ -44,13 +44,14 @@ int rwnmr_place_walkers(const uint64_t *blocks, int32_t nx, int32_t ny, int32_t 
                         int32_t deviation, int32_t shift, uint64_t seed, int64_t n, int32_t *x0, int32_t *y0,
                         int32_t *z0, uint64_t *seed0, rwnmr_placement_info *info);
 
-/* Configuration files (rwnmr / uct / cpmg / pfgse) read with the reference's rules (default file
+/* Configuration files (rwnmr / uct / cpmg / pfgse / multitau) read with the reference's rules (default file
  * under <config_root>default/, then the user file; "KEY: value" lines) and returned as JSON in out
  * (cap bytes). Returns the JSON length, or -1 with the error message in out. */
 int rwnmr_config_json(const char *kind, const char *config_root, const char *user_path, char *out, int cap);
 
 /* The command-line driver, the reference's RWNMR (App/rwnmrApp.cpp, Utils/ArgsParser.cpp):
  *   -rwconfig FILE -uctconfig FILE cpmg [-config FILE] pfgse [-config FILE]
+ *   multitau [-config MTFILE CPMGFILE | -mtconfig MTFILE | -cpmgconfig CPMGFILE]
  * plus --config-root, --synthetic, --labels/--shape, --device, --quiet. Writes the reference's
  * output files under ./db/<NAME>/. Returns the process exit code. */
 int rwnmr_cli_main(int argc, const char *const *argv);

@@ -291,6 +291,18 @@ class RefSim:
             raise ValueError("cap too small")
         return dict(raw=raw[:n].copy(), signal=out[:n].copy(), times=times[:n].copy(), map_collisions=mc)
 
+    def multitau(self, cpmg_text, multitau_text, cap=256):
+        """The reference's NMR_multitau::run on CPU; returns steps per echo, echo times, first echoes."""
+        L = self.lib()
+        L.ref_multitau.restype = ctypes.c_int
+        steps = np.zeros(cap, np.uint32)
+        times, amps = np.zeros(cap), np.zeros(cap)
+        n = L.ref_multitau(_vp(self.h), cpmg_text.encode(), multitau_text.encode(), cap, _ptr(steps), _ptr(times),
+                           _ptr(amps))
+        if n < 0:
+            raise ValueError("ref_multitau failed")
+        return dict(steps=steps[:n].copy(), times=times[:n].copy(), amps=amps[:n].copy())
+
     def pfgse(self, pulse_width, gmax, n_g, time_seq, n_t, t_min=0.0, t_max=1.0, t_values=None, apply_bulk=False,
               threshold_type="samples", threshold_value=None, threshold_window=1, cap=256):
         L = self.lib()
@@ -310,6 +322,33 @@ class RefSim:
             raise ValueError("cap too small")
         return dict(Mkt=Mkt[: nd * n_g].reshape(nd, n_g).copy(), steps=steps[:nd].copy(), dsat=dsat[:nd].copy(),
                     dmsd=dmsd[:nd].copy(), kvec=kvec.reshape(n_g, 3), delta=delta[:nd].copy())
+
+
+def _ref_pfgse_sampling(sim, samples, pulse_width, gmax, n_g, t_values, apply_bulk=False, threshold_type="samples",
+                        threshold_value=None, cap=64):
+    L = sim.lib()
+    L.ref_pfgse_sampling.restype = ctypes.c_int
+    tv = np.ascontiguousarray(t_values, np.float64)
+    if threshold_value is None:
+        threshold_value = n_g
+    Mkt, Mstd, lhs, lhs_std = (np.zeros(cap * n_g) for _ in range(4))
+    steps = np.zeros(cap, np.int32)
+    dsat, dmsd, delta, dsat_err, dsat_std, dmsd_std = (np.zeros(cap) for _ in range(6))
+    kvec = np.zeros(n_g * 3)
+    nd = L.ref_pfgse_sampling(_vp(sim.h), int(samples), ctypes.c_double(pulse_width), ctypes.c_double(gmax[0]),
+                              ctypes.c_double(gmax[1]), ctypes.c_double(gmax[2]), n_g, b"manual", len(tv), _ptr(tv),
+                              int(apply_bulk), threshold_type.encode(), ctypes.c_double(threshold_value), cap, _ptr(Mkt),
+                              _ptr(steps), _ptr(dsat), _ptr(dmsd), _ptr(kvec), _ptr(delta), _ptr(Mstd), _ptr(lhs),
+                              _ptr(lhs_std), _ptr(dsat_err), _ptr(dsat_std), _ptr(dmsd_std))
+    if nd < 0:
+        raise ValueError("cap too small")
+    r = lambda a: a[: nd * n_g].reshape(nd, n_g).copy()  # noqa: E731
+    return dict(Mkt=r(Mkt), Mstd=r(Mstd), lhs=r(lhs), lhs_std=r(lhs_std), steps=steps[:nd].copy(), dsat=dsat[:nd].copy(),
+                dsat_err=dsat_err[:nd].copy(), dsat_std=dsat_std[:nd].copy(), dmsd=dmsd[:nd].copy(),
+                dmsd_std=dmsd_std[:nd].copy(), delta=delta[:nd].copy())
+
+
+RefSim.pfgse_sampling = _ref_pfgse_sampling
 
 
 def ref_uniform_field(labels, resolution, gradient, direction):

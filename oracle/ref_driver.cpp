@@ -29,6 +29,7 @@
 #include "NMR_Simulation/NMR_cpmg.h"
 #include "NMR_Simulation/NMR_pfgse.h"
 #include "NMR_Simulation/InternalField.h"
+#include "NMR_Simulation/NMR_multitau.h"
 #include "Walker/walker.h"
 
 // ---------------------------------------------------------------------------------------------
@@ -376,43 +377,66 @@ int ref_cpmg(void *hv, double obs_time, int apply_bulk, double *raw, double *out
     return n;
 }
 
+// The reference's multitau sequence on CPU (NMR_multitau::run, NMR_multitau.cpp:187-204): one
+// CPMG per echo time (setTauSequence), each run's first normalised echo kept. cpmg_text and
+// multitau_text become default/cpmg.config and default/multitau.config. Writes steps[k], times[k]
+// and amps[k]; returns the number of echo times, or -1 if cap is too small.
+int ref_multitau(void *hv, const char *cpmg_text, const char *multitau_text, int cap, uint32_t *steps, double *times,
+                 double *amps)
+{
+    ref_handle *h = (ref_handle *)hv;
+    NMR_Simulation &s = *h->sim;
+    write_file(h->workdir + "/config/default/cpmg.config", cpmg_text);
+    write_file(h->workdir + "/config/default/multitau.config", multitau_text);
+    cwd_guard g(h->workdir);
+    multitau_config mcfg(std::string(CONFIG_ROOT) + MULTITAU_CONFIG_DEFAULT);
+    cpmg_config ccfg(std::string(CONFIG_ROOT) + CPMG_CONFIG_DEFAULT);
+    const uint32_t spe = s.getStepsPerEcho();
+    NMR_multitau mt(s, mcfg, ccfg);
+    mt.run();
+    s.setNumberOfStepsPerEcho(spe); // multitau leaves the last echo time's steps behind
+    const int n = (int)mt.signalAmps.size();
+    if (n > cap || mt.requiredSteps.size() != (size_t)n || mt.signalTimes.size() != (size_t)n) return -1;
+    for (int k = 0; k < n; k++)
+    {
+        steps[k] = mt.requiredSteps[k];
+        times[k] = mt.signalTimes[k];
+        amps[k] = mt.signalAmps[k];
+    }
+    return n;
+}
+
 // The reference's PFGSE sequence on CPU (NMR_PFGSE::run, NMR_pfgse.cpp:98-131, without file
 // output): initial mapping walk to the longest time, then per exposure time the CPU simulation
 // (simulation_omp, NMR_pfgse.cpp:1658-1806), bulk, and the D(t) recoveries.
 //   Mkt [n_delta * n_g]: normalised M(k, Delta) after bulk;  steps[n_delta]: RW steps per Delta;
 //   dsat/dmsd [n_delta]; kvec [n_g * 3]; delta_out [n_delta]: exposure times used.
 // Returns n_delta, or -1 if cap_delta is too small.
-int ref_pfgse(void *hv, double pulse_width, double gx, double gy, double gz, int n_g, const char *time_seq, int n_t,
-              double t_min, double t_max, const double *t_values, int apply_bulk, const char *threshold_type,
-              double threshold_value, int threshold_window, int cap_delta, double *Mkt, int32_t *steps, double *dsat,
-              double *dmsd, double *kvec, double *delta_out)
+} // extern "C"
+
+// Outputs of one PFGSE sequence run beyond the sequence's own vectors (walker-sampling statistics).
+struct pfgse_extra
 {
-    ref_handle *h = (ref_handle *)hv;
+    double *Mstd, *lhs, *lhs_std, *dsat_err, *dsat_std, *dmsd_std;
+};
+
+static int run_pfgse_sequence(ref_handle *h, const std::string &cfg_text, int n_g, int cap_delta, int samples,
+                              double *Mkt, int32_t *steps, double *dsat, double *dmsd, double *kvec, double *delta_out,
+                              const pfgse_extra *x)
+{
     NMR_Simulation &s = *h->sim;
-    std::ostringstream c;
-    c << "APPLY_BULK: " << (apply_bulk ? "true" : "false") << "\n";
-    c << "PULSE_WIDTH: " << fmt_double(pulse_width) << "\n";
-    c << "MAX_GRADIENT: {" << fmt_double(gx) << ", " << fmt_double(gy) << ", " << fmt_double(gz) << "}\n";
-    c << "GRADIENT_SAMPLES: " << n_g << "\n";
-    c << "TIME_SEQ: " << time_seq << "\n";
-    c << "TIME_SAMPLES: " << n_t << "\n";
-    if (std::string(time_seq) == "manual")
-    {
-        c << "TIME_VALUES: {";
-        for (int i = 0; i < n_t; i++) c << (i ? ", " : "") << fmt_double(t_values[i]);
-        c << "}\n";
-    }
-    c << "TIME_MIN: " << fmt_double(t_min) << "\nTIME_MAX: " << fmt_double(t_max) << "\n";
-    c << "APPLY_SCALE_FACTOR: false\nINSPECTION_LENGTH: 1.0\n";
-    c << "THRESHOLD_TYPE: " << threshold_type << "\nTHRESHOLD_VALUE: " << fmt_double(threshold_value) << "\n";
-    c << "THRESHOLD_WINDOW: " << threshold_window << "\n";
-    c << "ALLOW_WALKER_SAMPLING: false\nAPPLY_ABSORPTION: false\nSAVE_MODE: false\n";
-    write_file(h->workdir + "/config/default/pfgse.config", c.str());
+    write_file(h->workdir + "/config/default/pfgse.config", cfg_text);
     cwd_guard g(h->workdir);
+    const uint old_samples = s.walkerSamples;
+    if (samples > 0) s.walkerSamples = (uint)samples;
     pfgse_config cfg(std::string(CONFIG_ROOT) + PFGSE_CONFIG_DEFAULT);
     NMR_PFGSE pf(s, cfg);
     int nd = (int)pf.exposureTimes.size();
-    if (nd > cap_delta) return -1;
+    if (nd > cap_delta)
+    {
+        s.walkerSamples = old_samples;
+        return -1;
+    }
     for (int j = 0; j < n_g; j++)
     {
         kvec[3 * j + 0] = pf.vecK[j].getX();
@@ -442,10 +466,78 @@ int ref_pfgse(void *hv, double pulse_width, double gx, double gy, double gz, int
         dsat[t] = pf.getD_sat();
         dmsd[t] = pf.getD_msd();
         delta_out[t] = pf.getExposureTime();
+        if (x)
+        {
+            for (int j = 0; j < n_g; j++)
+            {
+                x->Mstd[(size_t)t * n_g + j] = pf.Mkt_stdev[j];
+                x->lhs[(size_t)t * n_g + j] = pf.LHS[j];
+                x->lhs_std[(size_t)t * n_g + j] = pf.LHS_stdev[j];
+            }
+            x->dsat_err[t] = pf.getD_sat_error();
+            x->dsat_std[t] = pf.getD_sat_stdev();
+            x->dmsd_std[t] = pf.getD_msd_stdev();
+        }
         pf.incrementCurrentTime();
     }
     mallopt(M_PERTURB, 0);
+    s.walkerSamples = old_samples;
     return nd;
+}
+
+static std::string pfgse_text(double pulse_width, double gx, double gy, double gz, int n_g, const char *time_seq, int n_t,
+                              double t_min, double t_max, const double *t_values, int apply_bulk,
+                              const char *threshold_type, double threshold_value, int threshold_window,
+                              bool allow_sampling)
+{
+    std::ostringstream c;
+    c << "APPLY_BULK: " << (apply_bulk ? "true" : "false") << "\n";
+    c << "PULSE_WIDTH: " << fmt_double(pulse_width) << "\n";
+    c << "MAX_GRADIENT: {" << fmt_double(gx) << ", " << fmt_double(gy) << ", " << fmt_double(gz) << "}\n";
+    c << "GRADIENT_SAMPLES: " << n_g << "\n";
+    c << "TIME_SEQ: " << time_seq << "\n";
+    c << "TIME_SAMPLES: " << n_t << "\n";
+    if (std::string(time_seq) == "manual")
+    {
+        c << "TIME_VALUES: {";
+        for (int i = 0; i < n_t; i++) c << (i ? ", " : "") << fmt_double(t_values[i]);
+        c << "}\n";
+    }
+    c << "TIME_MIN: " << fmt_double(t_min) << "\nTIME_MAX: " << fmt_double(t_max) << "\n";
+    c << "APPLY_SCALE_FACTOR: false\nINSPECTION_LENGTH: 1.0\n";
+    c << "THRESHOLD_TYPE: " << threshold_type << "\nTHRESHOLD_VALUE: " << fmt_double(threshold_value) << "\n";
+    c << "THRESHOLD_WINDOW: " << threshold_window << "\n";
+    c << "ALLOW_WALKER_SAMPLING: " << (allow_sampling ? "true" : "false") << "\nAPPLY_ABSORPTION: false\nSAVE_MODE: false\n";
+    return c.str();
+}
+
+extern "C" {
+
+int ref_pfgse(void *hv, double pulse_width, double gx, double gy, double gz, int n_g, const char *time_seq, int n_t,
+              double t_min, double t_max, const double *t_values, int apply_bulk, const char *threshold_type,
+              double threshold_value, int threshold_window, int cap_delta, double *Mkt, int32_t *steps, double *dsat,
+              double *dmsd, double *kvec, double *delta_out)
+{
+    return run_pfgse_sequence((ref_handle *)hv,
+                              pfgse_text(pulse_width, gx, gy, gz, n_g, time_seq, n_t, t_min, t_max, t_values, apply_bulk,
+                                         threshold_type, threshold_value, threshold_window, false),
+                              n_g, cap_delta, 0, Mkt, steps, dsat, dmsd, kvec, delta_out, nullptr);
+}
+
+// The same sequence with ALLOW_WALKER_SAMPLING: true and WALKER_SAMPLES = samples
+// (recoverDsatWithSampling / recoverDmsdWithSampling, NMR_pfgse.cpp:876-1097, 1173-1290). Extra
+// outputs per exposure time: Mstd, lhs, lhs_std [n_delta * n_g]; dsat_err, dsat_std, dmsd_std [n_delta].
+int ref_pfgse_sampling(void *hv, int samples, double pulse_width, double gx, double gy, double gz, int n_g,
+                       const char *time_seq, int n_t, const double *t_values, int apply_bulk, const char *threshold_type,
+                       double threshold_value, int cap_delta, double *Mkt, int32_t *steps, double *dsat, double *dmsd,
+                       double *kvec, double *delta_out, double *Mstd, double *lhs, double *lhs_std, double *dsat_err,
+                       double *dsat_std, double *dmsd_std)
+{
+    pfgse_extra x{Mstd, lhs, lhs_std, dsat_err, dsat_std, dmsd_std};
+    return run_pfgse_sequence((ref_handle *)hv,
+                              pfgse_text(pulse_width, gx, gy, gz, n_g, time_seq, n_t, 0.0, 1.0, t_values, apply_bulk,
+                                         threshold_type, threshold_value, 1, true),
+                              n_g, cap_delta, samples, Mkt, steps, dsat, dmsd, kvec, delta_out, &x);
 }
 
 } // extern "C"

@@ -1,7 +1,8 @@
 // Command-line application: the reference's RWNMR driver (src/backend/main.cpp, App/rwnmrApp.cpp,
 // Utils/ArgsParser.cpp) over the GPU engine.
 //
-//   rwnmr_gb300 [-rwconfig FILE] [-uctconfig FILE] cpmg [-config FILE] pfgse [-config FILE] ...
+//   rwnmr_gb300 [-rwconfig FILE] [-uctconfig FILE] cpmg [-config FILE] pfgse [-config FILE]
+//               multitau [-config MT CPMG | -mtconfig MT | -cpmgconfig CPMG] ...
 //
 // Commands run in the order given, on one simulation (image + walkers), exactly as the reference's
 // rwnmrApp::exec does. Options beyond the reference's:
@@ -38,6 +39,7 @@ std::vector<double> csv_numbers(const std::string &s)
 int usage()
 {
     std::cerr << "usage: rwnmr_gb300 [-rwconfig FILE] [-uctconfig FILE] [cpmg [-config FILE]] [pfgse [-config FILE]]\n"
+                 "       [multitau [-config MTFILE CPMGFILE | -mtconfig MTFILE | -cpmgconfig CPMGFILE]]\n"
                  "       [--config-root DIR] [--synthetic NX,NY,NZ,RMIN,RMAX,POROSITY,PHASES,SEED]\n"
                  "       [--labels FILE --shape NZ,NY,NX] [--device N] [--quiet]\n";
     return 2;
@@ -47,7 +49,11 @@ int usage()
 int cli_main(int argc, const char *const *argv)
 {
     std::string rw_path = "default", uct_path = "default", root = "./config/", labels_path;
-    std::vector<std::pair<std::string, std::string>> commands; // (command, config path)
+    struct Command
+    {
+        std::string name, path = "default", path2 = "default"; // path2: multitau's cpmg config
+    };
+    std::vector<Command> commands;
     std::vector<double> synth, shape;
     int device = 0;
     bool quiet = false;
@@ -59,15 +65,38 @@ int cli_main(int argc, const char *const *argv)
         };
         if (a == "-rwconfig") next(rw_path);
         else if (a == "-uctconfig") next(uct_path);
-        else if (a == "cpmg" || a == "pfgse" || a == "ga" || a == "multitau")
+        else if (a == "cpmg" || a == "pfgse" || a == "ga")
         {
-            std::string path = "default";
+            Command c{a};
             if (i + 2 < argc && std::string(argv[i + 1]) == "-config")
             {
-                path = argv[i + 2];
+                c.path = argv[i + 2];
                 i += 2;
             }
-            commands.push_back({a, path});
+            commands.push_back(c);
+        }
+        else if (a == "multitau")
+        {
+            // multitau [-config MT CPMG | -mtconfig MT | -cpmgconfig CPMG] (Utils/ArgsParser.cpp:104-145)
+            Command c{a};
+            const std::string flag = i + 1 < argc ? argv[i + 1] : "";
+            if (flag == "-config" && i + 3 < argc)
+            {
+                c.path = argv[i + 2];
+                c.path2 = argv[i + 3];
+                i += 3;
+            }
+            else if (flag == "-mtconfig" && i + 2 < argc)
+            {
+                c.path = argv[i + 2];
+                i += 2;
+            }
+            else if (flag == "-cpmgconfig" && i + 2 < argc)
+            {
+                c.path2 = argv[i + 2];
+                i += 2;
+            }
+            commands.push_back(c);
         }
         else if (a == "--config-root")
         {
@@ -157,13 +186,13 @@ int cli_main(int argc, const char *const *argv)
         std::cerr << err << std::endl;
         return 1;
     }
-    if (rw.save_img_info) sim.save_info();
+    sim.save_info(); // NMR_Simulation::save (rwnmrApp.cpp:68): SimInfo + the SAVE_IMG_INFO / SAVE_BINIMG / SAVE_WALKERS files
     for (auto &cmd : commands)
     {
-        if (cmd.first == "cpmg")
+        if (cmd.name == "cpmg")
         {
             CpmgConfig c;
-            if (!load_cpmg(root, cmd.second == "default" ? root + "default/cpmg.config" : cmd.second, c, err))
+            if (!load_cpmg(root, cmd.path == "default" ? root + "default/cpmg.config" : cmd.path, c, err))
             {
                 std::cerr << err << std::endl;
                 return 1;
@@ -175,10 +204,10 @@ int cli_main(int argc, const char *const *argv)
                 return 1;
             }
         }
-        else if (cmd.first == "pfgse")
+        else if (cmd.name == "pfgse")
         {
             PfgseConfig c;
-            if (!load_pfgse(root, cmd.second == "default" ? root + "default/pfgse.config" : cmd.second, c, err))
+            if (!load_pfgse(root, cmd.path == "default" ? root + "default/pfgse.config" : cmd.path, c, err))
             {
                 std::cerr << err << std::endl;
                 return 1;
@@ -190,12 +219,25 @@ int cli_main(int argc, const char *const *argv)
                 return 1;
             }
         }
-        else if (cmd.first == "ga")
+        else if (cmd.name == "ga")
             std::cout << "-- GA is under construction." << std::endl; // as the reference (App/rwnmrApp.cpp:204-207)
         else
         {
-            std::cerr << "multitau is not part of this build" << std::endl;
-            return 1;
+            // rwnmrApp::MultiTau (App/rwnmrApp.cpp:129-150)
+            MultitauConfig mc;
+            CpmgConfig cc;
+            if (!load_multitau(root, cmd.path, mc, err) ||
+                !load_cpmg(root, cmd.path2 == "default" ? root + "default/cpmg.config" : cmd.path2, cc, err))
+            {
+                std::cerr << err << std::endl;
+                return 1;
+            }
+            MultitauSequence seq(sim, mc, cc);
+            if (!seq.run(err))
+            {
+                std::cerr << err << std::endl;
+                return 1;
+            }
         }
     }
     return 0;
@@ -238,6 +280,12 @@ int rwnmr_config_json(const char *kind, const char *config_root, const char *use
     {
         PfgseConfig c;
         ok = load_pfgse(root, user, c, err);
+        js = to_json(c);
+    }
+    else if (k == "multitau")
+    {
+        MultitauConfig c;
+        ok = load_multitau(root, user, c, err);
         js = to_json(c);
     }
     else

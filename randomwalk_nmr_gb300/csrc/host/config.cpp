@@ -270,6 +270,39 @@ bool load_cpmg(const std::string &root, const std::string &user, CpmgConfig &c, 
     return load_two(root, "cpmg", kCpmgDefaults, user, false, h, err);
 }
 
+bool load_multitau(const std::string &root, const std::string &user, MultitauConfig &c, std::string &err)
+{
+    Handler h = [&](const std::string &k, const std::string &v) {
+        int i;
+        double d;
+        if (k == "TAU_MIN") { if (to_d(v, d)) c.tau_min = d; }
+        else if (k == "TAU_MAX") { if (to_d(v, d)) c.tau_max = d; }
+        else if (k == "TAU_POINTS") { if (to_i(v, i)) c.tau_points = i; }
+        else if (k == "TAU_VALUES")
+        {
+            c.tau_values = parse_list(v, true);
+            std::sort(c.tau_values.begin(), c.tau_values.end());
+        }
+        else if (k == "TAU_SCALE") c.tau_scale = (v == "log" || v == "linear") ? v : "manual";
+        else if (k == "COMPLETE_DECAY") c.complete_decay = v == "true" || v == "True" || v == "TRUE";
+        else if (k == "SAVE_MODE") c.save_mode = is_true(v);
+        else if (k == "SAVE_DECAY") c.save_decay = is_true(v);
+        else if (k == "SAVE_WALKERS") c.save_walkers = is_true(v);
+        else if (k == "SAVE_HISTOGRAM") c.save_histogram = is_true(v);
+        else if (k == "SAVE_HISTOGRAM_LIST") c.save_histogram_list = is_true(v);
+    };
+    const std::string cpmg_default = root + "default/cpmg.config";
+    if (!scan_file(cpmg_default, h)) scan_text(kCpmgDefaults, h);
+    const std::string path = (user.empty() || user == "default") ? root + "default/multitau.config" : user;
+    if (path == cpmg_default) return true;
+    if (!scan_file(path, h))
+    {
+        err = "could not open multitau config file " + path;
+        return false;
+    }
+    return true;
+}
+
 bool load_pfgse(const std::string &root, const std::string &user, PfgseConfig &c, std::string &err)
 {
     Handler h = [&](const std::string &k, const std::string &v) {
@@ -377,6 +410,18 @@ std::string to_json(const PfgseConfig &c)
       << ",\"THRESHOLD_TYPE\":" << q(c.threshold_type) << ",\"THRESHOLD_VALUE\":" << num(c.threshold_value)
       << ",\"THRESHOLD_WINDOW\":" << c.threshold_window << ",\"ALLOW_WALKER_SAMPLING\":" << tf(c.allow_walker_sampling)
       << ",\"APPLY_ABSORPTION\":" << tf(c.apply_absorption) << ",\"SAVE_PFGSE\":" << tf(c.save_pfgse) << "}";
+    return o.str();
+}
+
+std::string to_json(const MultitauConfig &c)
+{
+    std::ostringstream o;
+    o << "{\"TAU_MIN\":" << num(c.tau_min) << ",\"TAU_MAX\":" << num(c.tau_max) << ",\"TAU_POINTS\":" << c.tau_points
+      << ",\"TAU_VALUES\":" << arr(c.tau_values) << ",\"TAU_SCALE\":" << q(c.tau_scale)
+      << ",\"COMPLETE_DECAY\":" << tf(c.complete_decay) << ",\"SAVE_MODE\":" << tf(c.save_mode)
+      << ",\"SAVE_DECAY\":" << tf(c.save_decay) << ",\"SAVE_WALKERS\":" << tf(c.save_walkers)
+      << ",\"SAVE_HISTOGRAM\":" << tf(c.save_histogram) << ",\"SAVE_HISTOGRAM_LIST\":" << tf(c.save_histogram_list)
+      << "}";
     return o.str();
 }
 

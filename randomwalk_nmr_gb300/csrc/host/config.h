@@ -93,6 +93,20 @@ struct PfgseConfig
     bool save_mode = true, save_pfgse = true, save_walkers = false, save_histogram = true, save_histogram_list = false;
 };
 
+// multitau.config (ConfigFiles/multitau_config.cpp:65-178). The reference leaves every field without
+// a default (its constructor reads the cpmg default file by mistake, so only the SAVE_* keys of
+// cpmg.config reach it); these defaults stand in for the unset values.
+struct MultitauConfig
+{
+    double tau_min = 0.0, tau_max = 0.0;
+    int tau_points = 0;
+    std::vector<double> tau_values;
+    std::string tau_scale = "linear";
+    bool complete_decay = false;
+    bool save_mode = false, save_decay = false, save_walkers = false, save_histogram = false,
+         save_histogram_list = false;
+};
+
 // Reads the default file (config_root + "default/<kind>.config") and then the user file, like
 // the reference: rwnmr/uct/cpmg skip the user file when it is the default file itself; pfgse reads
 // both regardless. A missing default file falls back to the values the reference ships.
@@ -104,6 +118,9 @@ bool load_rwnmr(const std::string &config_root, const std::string &user, RwnmrCo
 bool load_uct(const std::string &config_root, const std::string &user, UctConfig &c, std::string &err);
 bool load_cpmg(const std::string &config_root, const std::string &user, CpmgConfig &c, std::string &err);
 bool load_pfgse(const std::string &config_root, const std::string &user, PfgseConfig &c, std::string &err);
+// multitau: the reference reads config_root + "default/cpmg.config" first (multitau_config.cpp:16-22),
+// then the user file (config_root + "default/multitau.config" when "default").
+bool load_multitau(const std::string &config_root, const std::string &user, MultitauConfig &c, std::string &err);
 
 // PFGSE exposure times (pfgse_config.cpp:191-240): log = 10^linspace, linear, manual (sorted).
 std::vector<double> pfgse_time_samples(const PfgseConfig &c);
@@ -112,5 +129,6 @@ std::string to_json(const RwnmrConfig &c);
 std::string to_json(const UctConfig &c);
 std::string to_json(const CpmgConfig &c);
 std::string to_json(const PfgseConfig &c);
+std::string to_json(const MultitauConfig &c);
 
 } // namespace rwnmr_host

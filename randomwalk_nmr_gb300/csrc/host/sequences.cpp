@@ -365,17 +365,41 @@ void Simulation::save_info() const
     f << "Walkers pore occupancy in simulation: " << occupancy * 100.0 << "%\n";
     f << "Initial seed: " << initial_seed << "\n";
     f << "GPU usage: ON (rwnmr_gb300, sm_103a)\n";
-    std::ofstream g(sim_dir + "/ImageInfo.txt");
-    g << "image path: " << img.source << "\n";
-    g << "width(x): " << img.nx << "\nheight(y): " << img.ny << "\ndepth(z): " << img.nz << "\n";
-    g << "resolution: " << resolution << "\nvoxel shift: " << (1 << shift) << "\nstep length: " << voxel_res << "\n";
-    g << "porosity: " << porosity << "\nSVp: " << svp << "\n";
+    // saveImageInfo (NMR_Simulation.cpp:1644-1672)
+    if (rw.save_img_info)
+    {
+        std::ofstream g(sim_dir + "/ImageInfo.txt");
+        g << "image path: " << img.source << "\n";
+        g << "width(x): " << img.nx << "\nheight(y): " << img.ny << "\ndepth(z): " << img.nz << "\n";
+        g << "resolution: " << resolution << "\nvoxel shift: " << (1 << shift) << "\nstep length: " << voxel_res << "\n";
+        g << "porosity: " << porosity << "\nSVp: " << svp << "\n";
+    }
+    // saveBitBlock -> fileHandler::writeBitBlockObject3D (FileHandler/fileHandler.cpp:192-235)
+    if (rw.save_binimg)
+    {
+        const int bc = (img.nx + 3) / 4, br = (img.ny + 3) / 4, bd = (img.nz + 3) / 4;
+        std::ofstream b(sim_dir + "/NMR_binImage.txt");
+        b << "blocks, bRows, bColumns, bDepth, imgRows, imgColumns, imgDepth, \n";
+        b << img.blocks.size() << ", " << br << ", " << bc << ", " << bd << ", " << img.ny << ", " << img.nx << ", "
+          << img.nz << "\n\nblockID, blockData\n";
+        for (size_t k = 0; k < img.blocks.size(); k++) b << k << ", " << img.blocks[k] << "\n";
+    }
+    // saveWalkers (NMR_Simulation.cpp:1674-1712): the walkers as created, before any walk
+    if (rw.save_walkers)
+    {
+        std::ofstream w(sim_dir + "/walkers.csv");
+        w << std::setprecision(6);
+        w << "PositionXi,PositionYi,PositionZi,PositionXf,PositionYf,PositionZf,Collisions,XIRate,Energy,RNGSeed\n";
+        for (size_t i = 0; i < x0.size(); i++)
+            w << x0[i] << "," << y0[i] << "," << z0[i] << "," << x0[i] << "," << y0[i] << "," << z0[i] << ",0,0,1,"
+              << seed0[i] << "\n";
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
 bool CpmgSequence::set(std::string &err)
 {
-    name = "/NMR_cpmg_t=" + trimmed_time(cfg.obs_time) + "ms";
+    name = parent + "/NMR_cpmg_t=" + trimmed_time(cfg.obs_time) + "ms" + suffix;
     mkdirs(sim.db_path + sim.rw.name + "/" + name);
     dir = sim.db_path + sim.rw.name + "/" + name;
     sim.set_time_framework_time(cfg.obs_time);
@@ -392,6 +416,7 @@ bool CpmgSequence::set(std::string &err)
     // The reference always runs the collision-mapping walk here (NMR_cpmg.cpp:134). With uniform
     // relaxivity nothing but the histogram / walker outputs depends on it, so it runs only when one
     // of those is requested.
+    if (!map) return true;
     const bool need_map = sim.rw.rho_type == "sigmoid" || cfg.method == "histogram" ||
                           (cfg.save_mode && (cfg.save_histogram || cfg.save_histogram_list || cfg.save_walkers));
     if (need_map && !sim.map_simulation(err)) return false;
@@ -559,10 +584,12 @@ void CpmgSequence::save() const
         rwnmr_walkers_download(sim.ctx, x.data(), y.data(), z.data(), nullptr, nullptr);
         f << "PositionXi,PositionYi,PositionZi,PositionXf,PositionYf,PositionZf,Collisions,XIRate,Energy,RNGSeed\n";
         const double fd = sim.decrease_factor(sim.rho_phase[0]);
+        const bool per_walker = sim.walker_dfactors.size() == x.size();
         for (size_t i = 0; i < x.size(); i++)
             f << sim.x0[i] << "," << sim.y0[i] << "," << sim.z0[i] << "," << x[i] << "," << y[i] << "," << z[i] << ","
-              << sim.collisions[i] << "," << sim.xi_rate[i] << "," << std::pow(fd, (double)sim.collisions[i]) << ","
-              << sim.seed0[i] << "\n";
+              << sim.collisions[i] << "," << sim.xi_rate[i] << ","
+              << std::pow(per_walker ? sim.walker_dfactors[i] : fd, (double)sim.collisions[i]) << "," << sim.seed0[i]
+              << "\n";
     }
     if (cfg.save_histogram && !sim.histogram.bins.empty())
     {
@@ -589,6 +616,126 @@ bool CpmgSequence::run(std::string &err)
     save();
     sim.log("- CPMG: " + std::to_string(sim.echoes) + " echoes x " + std::to_string(sim.rw.steps_per_echo) +
             " steps, walk " + std::to_string(kernel_ms) + " ms on the GPU");
+    return true;
+}
+
+// ---------------------------------------------------------------------------------------------
+namespace
+{
+// std::to_string(v) cut `digits` places after the point of std::to_string(ref), the way
+// NMR_multitau::setName / setCPMG trim (the point is looked up in a second string).
+std::string trimmed_like(double v, double ref, int digits)
+{
+    const std::string s = std::to_string(v);
+    const size_t dot = std::to_string(ref).find('.');
+    return s.substr(0, dot == std::string::npos ? std::string::npos : dot + digits + 1);
+}
+} // namespace
+
+void MultitauSequence::set_tau_sequence()
+{
+    std::vector<double> t;
+    if (cfg.tau_scale == "manual") t = cfg.tau_values;
+    else
+    {
+        // linspace / logspace (NMR_multitau.cpp:51-78)
+        const int n = std::max(cfg.tau_points, 0);
+        const bool lg = cfg.tau_scale == "log";
+        const double a = lg ? std::log10(cfg.tau_min) : cfg.tau_min;
+        const double b = lg ? std::log10(cfg.tau_max) : cfg.tau_max;
+        const double step = (b - a) / ((double)n - 1.0);
+        for (int i = 0; i < n; i++)
+        {
+            const double x = a + step * i;
+            t.push_back(lg ? std::pow(10.0, x) : x);
+        }
+    }
+    required_steps.clear();
+    signal_times.clear();
+    uint32_t min_steps = 0;
+    for (double tau : t)
+    {
+        // ceil to whole steps, even, strictly increasing by at least two
+        int steps = (int)std::ceil(tau / sim.dt);
+        if (steps % 2 != 0) steps++;
+        if ((uint32_t)steps <= min_steps) steps = (int)min_steps + 2;
+        required_steps.push_back((uint32_t)steps);
+        min_steps = (uint32_t)steps;
+        signal_times.push_back(steps * sim.dt);
+    }
+}
+
+bool MultitauSequence::run(std::string &err)
+{
+    // setName (NMR_multitau.cpp:45-66)
+    std::string lo, hi, pts;
+    if (cfg.tau_scale == "manual")
+    {
+        if (cfg.tau_values.empty())
+        {
+            err = "TAU_SCALE manual needs TAU_VALUES";
+            return false;
+        }
+        lo = std::to_string(cfg.tau_values.front());
+        hi = std::to_string(cfg.tau_values.back());
+        pts = std::to_string(cfg.tau_values.size());
+    }
+    else
+    {
+        lo = std::to_string(cfg.tau_min);
+        hi = std::to_string(cfg.tau_max);
+        pts = std::to_string(cfg.tau_points);
+    }
+    {
+        const size_t dmin = std::to_string(cfg.tau_min).find('.'), dmax = std::to_string(cfg.tau_max).find('.');
+        lo = lo.substr(0, dmin == std::string::npos ? std::string::npos : dmin + 3);
+        hi = hi.substr(0, dmax == std::string::npos ? std::string::npos : dmax + 3);
+    }
+    name = "/NMR_multitau_min=" + lo + "ms_max=" + hi + "ms_pts=" + pts + "_scale=" + cfg.tau_scale;
+    mkdirs(sim.db_path + sim.rw.name + "/" + name);
+    dir = sim.db_path + sim.rw.name + "/" + name;
+    set_tau_sequence();
+    // a sigmoid relaxivity keeps each walker's current factor (none mapped yet: collision rate 0)
+    if (sim.rw.rho_type == "sigmoid" && sim.walker_dfactors.size() != sim.x0.size())
+    {
+        sim.collisions.assign(sim.x0.size(), 0);
+        if (!sim.upload_sigmoid_dfactors(1, err)) return false;
+    }
+    signal_amps.clear();
+    for (size_t k = 0; k < required_steps.size(); k++)
+    {
+        // setCPMG (NMR_multitau.cpp:119-131): te = required steps, one echo unless COMPLETE_DECAY
+        sim.rw.steps_per_echo = (int)required_steps[k];
+        CpmgSequence seq(sim, cpmg_cfg);
+        if (!cfg.complete_decay) seq.cfg.obs_time = signal_times[k];
+        seq.map = false;
+        seq.parent = name;
+        const double te = required_steps[k] * sim.dt;
+        seq.suffix = "_te=" + trimmed_like(te, te, 3);
+        if (!seq.set(err) || !seq.run_simulation(err)) return false;
+        kernel_ms += seq.kernel_ms;
+        if (seq.amps.size() > 1) signal_amps.push_back(seq.amps[1]);
+        if (cfg.complete_decay)
+        {
+            // saveCPMG (NMR_multitau.cpp:154-185): the multitau SAVE_* flags pick the files
+            seq.cfg.save_mode = true;
+            seq.cfg.save_walkers = cfg.save_walkers;
+            seq.cfg.save_histogram = cfg.save_histogram;
+            seq.cfg.save_histogram_list = cfg.save_histogram_list;
+            seq.cfg.save_decay = cfg.save_decay;
+            seq.save();
+        }
+    }
+    if (cfg.save_decay)
+    {
+        // writeDecay (NMR_multitau.cpp:221-248)
+        std::ofstream f = open_out(dir + "/multitau_decay.csv");
+        f << "echo_time,signal\n";
+        if (signal_times.size() == signal_amps.size())
+            for (size_t k = 0; k < signal_amps.size(); k++) f << signal_times[k] << "," << signal_amps[k] << "\n";
+    }
+    sim.log("- multitau: " + std::to_string(required_steps.size()) + " echo times, walks " + std::to_string(kernel_ms) +
+            " ms on the GPU");
     return true;
 }
 
@@ -689,6 +836,56 @@ bool PfgseSequence::run(std::string &err)
         return false;
     }
     kernel_ms = rwnmr_ctx_last_kernel_ms(S.ctx);
+    // Walker sampling (ALLOW_WALKER_SAMPLING with WALKER_SAMPLES > 1; NMR_pfgse.cpp:605-640, 876-1097,
+    // 1173-1290): the walkers split into WALKER_SAMPLES contiguous groups of N / WALKER_SAMPLES (the
+    // rest are left out), each group's M(k) and mean squared displacement computed on its own. The
+    // groups are walked as separate populations; every walker's trajectory is the same as in the
+    // full walk.
+    const int n_samples = S.rw.walker_samples;
+    const bool sampling = cfg.allow_walker_sampling && n_samples > 1;
+    const int64_t per = sampling ? (int64_t)S.x0.size() / n_samples : 0;
+    std::vector<double> Ms, es;      // [sample][n_delta][n_g], [sample][n_delta]
+    std::vector<uint64_t> msds;      // [sample][n_delta][3]
+    if (sampling)
+    {
+        Ms.assign((size_t)n_samples * nd * n_g, 0.0);
+        es.assign((size_t)n_samples * nd, 0.0);
+        msds.assign((size_t)n_samples * nd * 3, 0);
+        for (int smp = 0; smp < n_samples && rs == RWNMR_OK; smp++)
+        {
+            const size_t o = (size_t)smp * per;
+            rs = rwnmr_walkers_upload(S.ctx, per, S.x0.data() + o, S.y0.data() + o, S.z0.data() + o, S.seed0.data() + o);
+            if (rs == RWNMR_OK && p.dfactor == nullptr) rs = rwnmr_walkers_set_dfactor(S.ctx, S.walker_dfactors.data() + o);
+            if (rs == RWNMR_OK)
+                rs = rwnmr_pfgse_run(S.ctx, &p, &Ms[(size_t)smp * nd * n_g], &es[(size_t)smp * nd], &msds[(size_t)smp * nd * 3]);
+            kernel_ms += rwnmr_ctx_last_kernel_ms(S.ctx);
+        }
+        // the full population back in the engine for what runs next
+        if (rs == RWNMR_OK)
+            rs = rwnmr_walkers_upload(S.ctx, (int64_t)S.x0.size(), S.x0.data(), S.y0.data(), S.z0.data(), S.seed0.data());
+        if (rs == RWNMR_OK && p.dfactor == nullptr) rs = rwnmr_walkers_set_dfactor(S.ctx, S.walker_dfactors.data());
+        if (rs != RWNMR_OK)
+        {
+            err = std::string("PFGSE walker samples: ") + rwnmr_last_error(S.ctx);
+            return false;
+        }
+    }
+    auto mean_of = [](const std::vector<double> &v) {
+        double sum = 0.0;
+        for (double x : v) sum += x;
+        return sum / (double)v.size();
+    };
+    auto std_of = [](const std::vector<double> &v, double m) { // population deviation (NMR_pfgse.cpp:1863-1891)
+        double sum = 0.0;
+        for (double x : v) sum += (x - m) * (x - m);
+        return std::sqrt(sum / (double)v.size());
+    };
+    dsat_std.assign(nd, 0.0);
+    dmsd_std.assign(nd, 0.0);
+    dmsd_vec_std.assign((size_t)nd * 3, 0.0);
+    msd_vec_std.assign((size_t)nd * 3, 0.0);
+    m_std.assign((size_t)nd * n_g, 0.0);
+    lhs_std.assign((size_t)nd * n_g, 0.0);
     lhs.assign((size_t)nd * n_g, 0.0);
     rhs.assign((size_t)nd * n_g, 0.0);
     raw_noise.assign((size_t)nd * n_g, 0.0);
@@ -733,15 +930,60 @@ bool PfgseSequence::run(std::string &err)
         // recoverDsatWithoutSampling (NMR_pfgse.cpp:641-692)
         double *L = &lhs[(size_t)i * n_g];
         double *R = &rhs[(size_t)i * n_g];
-        std::vector<double> norm(n_g);
-        for (int j = 0; j < n_g; j++) norm[j] = M[j] / M[0];
+        auto lhs_of = [&](const double *m, double *out) {
+            std::vector<double> norm(n_g);
+            for (int j = 0; j < n_g; j++) norm[j] = m[j] / m[0];
+            for (int j = 0; j < n_g; j++)
+            {
+                const double ratio = norm[j] / norm[0];
+                out[j] = ratio > 1.0e-06 ? std::log(ratio) : std::log(1.0e-06);
+            }
+        };
+        lhs_of(M, L);
         for (int j = 0; j < n_g; j++)
         {
-            const double ratio = norm[j] / norm[0];
-            L[j] = ratio > 1.0e-06 ? std::log(ratio) : std::log(1.0e-06);
             const double k = std::sqrt(kvec[3 * j] * kvec[3 * j] + kvec[3 * j + 1] * kvec[3 * j + 1] +
                                        kvec[3 * j + 2] * kvec[3 * j + 2]);
             R[j] = (-1.0) * k * k * (delta - (cfg.pulse_width / 3.0));
+        }
+        // recoverDsatWithSampling (NMR_pfgse.cpp:876-1097): per-sample magnitudes (bulk, then noise of
+        // amplitude (N / samples) * NOISE_AMP drawn per sample when NOISE_AMP > 0), normalised per
+        // sample; the mean and population deviation over samples replace M and the LHS
+        std::vector<double> LS; // [sample][n_g]
+        if (sampling)
+        {
+            const double bm = cfg.apply_bulk ? std::exp((-1.0 / S.rw.bulk_time) * delta) : 1.0;
+            std::vector<double> Msmp((size_t)n_samples * n_g), Nsmp((size_t)n_samples * n_g, 0.0);
+            LS.assign((size_t)n_samples * n_g, 0.0);
+            for (int smp = 0; smp < n_samples; smp++)
+                for (int j = 0; j < n_g; j++)
+                    Msmp[(size_t)smp * n_g + j] = Ms[((size_t)smp * nd + i) * n_g + j] * bm;
+            if (noise_amp > 0.0)
+            {
+                const double m0 = N / (double)n_samples;
+                for (int smp = 0; smp < n_samples; smp++)
+                {
+                    std::normal_distribution<double> nd_(0.0, m0 * noise_amp);
+                    for (int j = 0; j < n_g; j++) Nsmp[(size_t)smp * n_g + j] = nd_(S.rng);
+                }
+                for (size_t k = 0; k < Msmp.size(); k++) Msmp[k] += Nsmp[k];
+            }
+            for (int smp = 0; smp < n_samples; smp++) lhs_of(&Msmp[(size_t)smp * n_g], &LS[(size_t)smp * n_g]);
+            for (int j = 0; j < n_g; j++)
+            {
+                std::vector<double> mv(n_samples), nv(n_samples), lv(n_samples);
+                for (int smp = 0; smp < n_samples; smp++)
+                {
+                    mv[smp] = Msmp[(size_t)smp * n_g + j];
+                    nv[smp] = Nsmp[(size_t)smp * n_g + j];
+                    lv[smp] = LS[(size_t)smp * n_g + j];
+                }
+                M[j] = mean_of(mv);
+                m_std[(size_t)i * n_g + j] = std_of(mv, M[j]);
+                raw_noise[(size_t)i * n_g + j] = mean_of(nv);
+                L[j] = mean_of(lv);
+                lhs_std[(size_t)i * n_g + j] = std_of(lv, L[j]);
+            }
         }
         int pts = n_g;
         int window = std::min(cfg.threshold_window, n_g);
@@ -790,37 +1032,91 @@ bool PfgseSequence::run(std::string &err)
             if (s <= n_g && s > 1) pts = s;
         }
         dsat_points[i] = pts;
-        std::vector<double> xs(R, R + pts), ys(L, L + pts);
-        double b, mse;
-        lsq_no_intercept(xs, ys, pts, b, mse);
-        dsat[i] = b;
-        dsat_err[i] = std::sqrt(mse * (((double)pts) / ((double)pts - 1.0)));
-        // recoverDmsdWithoutSampling (NMR_pfgse.cpp:1098-1171): exact integer sums of dR^2
-        const double r2 = S.voxel_res * S.voxel_res;
-        double tot = 0.0;
-        for (int a = 0; a < 3; a++)
+        std::vector<double> xs(R, R + pts);
+        if (!sampling)
         {
-            msd_vec[(size_t)i * 3 + a] = r2 * (double)msd[(size_t)i * 3 + a] / N;
-            dmsd_vec[(size_t)i * 3 + a] = msd_vec[(size_t)i * 3 + a] / (2.0 * delta);
-            tot += msd_vec[(size_t)i * 3 + a];
+            std::vector<double> ys(L, L + pts);
+            double b, mse;
+            lsq_no_intercept(xs, ys, pts, b, mse);
+            dsat[i] = b;
+            dsat_err[i] = std::sqrt(mse * (((double)pts) / ((double)pts - 1.0)));
         }
-        dmsd[i] = tot / (6.0 * delta);
+        else
+        {
+            std::vector<double> bs(n_samples), errs(n_samples);
+            for (int smp = 0; smp < n_samples; smp++)
+            {
+                std::vector<double> ys(&LS[(size_t)smp * n_g], &LS[(size_t)smp * n_g] + pts);
+                double b, mse;
+                lsq_no_intercept(xs, ys, pts, b, mse);
+                bs[smp] = b;
+                errs[smp] = std::sqrt(mse * (((double)pts) / ((double)pts - 1.0)));
+            }
+            dsat[i] = mean_of(bs);
+            dsat_err[i] = mean_of(errs);
+            dsat_std[i] = std_of(bs, dsat[i]);
+        }
+        // recoverDmsdWithoutSampling (NMR_pfgse.cpp:1098-1171): exact integer sums of dR^2; with
+        // sampling the per-sample values' means and population deviations (NMR_pfgse.cpp:1173-1290)
+        const double r2 = S.voxel_res * S.voxel_res;
+        if (!sampling)
+        {
+            double tot = 0.0;
+            for (int a = 0; a < 3; a++)
+            {
+                msd_vec[(size_t)i * 3 + a] = r2 * (double)msd[(size_t)i * 3 + a] / N;
+                dmsd_vec[(size_t)i * 3 + a] = msd_vec[(size_t)i * 3 + a] / (2.0 * delta);
+                tot += msd_vec[(size_t)i * 3 + a];
+            }
+            dmsd[i] = tot / (6.0 * delta);
+        }
+        else
+        {
+            std::vector<double> dm(n_samples), mv[3], dv[3];
+            for (int a = 0; a < 3; a++)
+            {
+                mv[a].resize(n_samples);
+                dv[a].resize(n_samples);
+            }
+            for (int smp = 0; smp < n_samples; smp++)
+            {
+                double tot = 0.0;
+                for (int a = 0; a < 3; a++)
+                {
+                    mv[a][smp] = r2 * (double)msds[((size_t)smp * nd + i) * 3 + a] / (double)per;
+                    dv[a][smp] = mv[a][smp] / (2.0 * delta);
+                    tot += mv[a][smp];
+                }
+                dm[smp] = tot / (6.0 * delta);
+            }
+            dmsd[i] = mean_of(dm);
+            dmsd_std[i] = std_of(dm, dmsd[i]);
+            for (int a = 0; a < 3; a++)
+            {
+                msd_vec[(size_t)i * 3 + a] = mean_of(mv[a]);
+                msd_vec_std[(size_t)i * 3 + a] = std_of(mv[a], msd_vec[(size_t)i * 3 + a]);
+                dmsd_vec[(size_t)i * 3 + a] = mean_of(dv[a]);
+                dmsd_vec_std[(size_t)i * 3 + a] = std_of(dv[a], dmsd_vec[(size_t)i * 3 + a]);
+            }
+        }
         if (cfg.save_mode && cfg.save_pfgse)
         {
             std::ofstream r = open_out(dir + "/PFGSE_results.csv", std::ios::app);
-            r << delta << "," << dsat[i] << "," << dsat_err[i] << "," << 0.0 << "," << pts << "," << dmsd[i] << "," << 0.0;
-            for (int a = 0; a < 3; a++) r << "," << dmsd_vec[(size_t)i * 3 + a] << "," << 0.0;
+            r << delta << "," << dsat[i] << "," << dsat_err[i] << "," << dsat_std[i] << "," << pts << "," << dmsd[i] << ","
+              << dmsd_std[i];
+            for (int a = 0; a < 3; a++) r << "," << dmsd_vec[(size_t)i * 3 + a] << "," << dmsd_vec_std[(size_t)i * 3 + a];
             r << "\n";
             std::ofstream e = open_out(dir + "/timesamples/echoes_" + std::to_string(i) + ".csv");
             e << "Idx,Gradient,NMR_signal(mean),NMR_signal(noise),NMR_signal(std),SAT_lhs(mean),SAT_lhs(std),SAT_rhs\n";
             for (int j = 0; j < n_g; j++)
-                e << j << "," << gradient[j] << "," << M[j] << "," << raw_noise[(size_t)i * n_g + j] << "," << 0.0 << ","
-                  << L[j] << "," << 0.0 << "," << R[j] << "\n";
+                e << j << "," << gradient[j] << "," << M[j] << "," << raw_noise[(size_t)i * n_g + j] << ","
+                  << m_std[(size_t)i * n_g + j] << "," << L[j] << "," << lhs_std[(size_t)i * n_g + j] << "," << R[j] << "\n";
             std::ofstream m = open_out(dir + "/timesamples/msd_" + std::to_string(i) + ".csv");
             m << "msdX(mean),msdX(std),msdY(mean),msdY(std),msdZ(mean),msdZ(std),DmsdX(mean),DmsdX(std),"
                  "DmsdY(mean),DmsdY(std),DmsdZ(mean),DmsdZ(std)\n";
-            for (int a = 0; a < 3; a++) m << msd_vec[(size_t)i * 3 + a] << "," << 0.0 << ",";
-            for (int a = 0; a < 3; a++) m << dmsd_vec[(size_t)i * 3 + a] << "," << 0.0 << (a < 2 ? "," : "");
+            for (int a = 0; a < 3; a++) m << msd_vec[(size_t)i * 3 + a] << "," << msd_vec_std[(size_t)i * 3 + a] << ",";
+            for (int a = 0; a < 3; a++)
+                m << dmsd_vec[(size_t)i * 3 + a] << "," << dmsd_vec_std[(size_t)i * 3 + a] << (a < 2 ? "," : "");
         }
         S.log("- D(" + std::to_string(delta) + " ms) {s&t} = " + std::to_string(dsat[i]) + ", {msd} = " +
               std::to_string(dmsd[i]));

@@ -93,6 +93,8 @@ class CpmgSequence
   public:
     Simulation &sim;
     CpmgConfig cfg;
+    std::string parent, suffix; // NMR_cpmg::setName(parent, sufix): directory nesting, e.g. under a multitau run
+    bool map = true;            // NMR_cpmg::setNMRTimeFramework(_map)
     std::string name, dir;
     std::vector<double> times, amps, raw, noise;
     std::vector<uint64_t> echo_collisions; // [echoes][phases]
@@ -117,6 +119,9 @@ class PfgseSequence
     // per exposure time
     std::vector<double> Mkt;             // [n_delta][n_g] un-normalised (sum E cos), after bulk and noise
     std::vector<double> esum, dsat, dsat_err, dmsd;
+    std::vector<double> dsat_std, dmsd_std;      // walker-sampling deviations (0 without sampling)
+    std::vector<double> m_std, lhs_std;          // [n_delta][n_g]
+    std::vector<double> msd_vec_std, dmsd_vec_std; // [n_delta][3]
     std::vector<int> dsat_points;
     std::vector<double> msd_vec, dmsd_vec; // [n_delta][3]
     std::vector<double> lhs, rhs, raw_noise; // [n_delta][n_g]
@@ -124,6 +129,23 @@ class PfgseSequence
     double kernel_ms = 0.0;
     PfgseSequence(Simulation &s, const PfgseConfig &c) : sim(s), cfg(c) {}
     bool run(std::string &err); // NMR_PFGSE::run (NMR_pfgse.cpp:98-131)
+};
+
+// Multi-echo-time CPMG (NMR_multitau.cpp:22-204): one CPMG per echo time te, keeping the first echo
+// of each (or each full decay with COMPLETE_DECAY), written to multitau_decay.csv.
+class MultitauSequence
+{
+  public:
+    Simulation &sim;
+    MultitauConfig cfg;
+    CpmgConfig cpmg_cfg;
+    std::string name, dir;
+    std::vector<uint32_t> required_steps; // steps per echo of each run
+    std::vector<double> signal_times, signal_amps;
+    double kernel_ms = 0.0;
+    MultitauSequence(Simulation &s, const MultitauConfig &c, const CpmgConfig &cc) : sim(s), cfg(c), cpmg_cfg(cc) {}
+    void set_tau_sequence(); // NMR_multitau::setTauSequence
+    bool run(std::string &err);
 };
 
 // The RWNMR command line (Utils/ArgsParser.cpp:10-152, App/rwnmrApp.cpp:106-231).

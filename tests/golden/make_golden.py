@@ -85,6 +85,22 @@ def main():
     out.update(pfgse_sig_Mkt=pf["Mkt"], pfgse_sig_dsat=pf["dsat"], pfgse_sig_dmsd=pf["dmsd"], pfgse_sig_dfactor=df)
     del rs5
 
+    # PFGSE with walker sampling (ALLOW_WALKER_SAMPLING, 4 samples). rho = 0 keeps every walker's
+    # energy at 1: the reference's CPU sampling sums weight sample s's walkers with the energies of
+    # sample 0 (NMR_pfgse.cpp:818, walkers[idx] for walkers[offset + idx]); its GPU path does not.
+    rs7 = RefSim(lab, 600, 11, rho=(0.0,), steps_per_echo=1, bulk_time=900.0)
+    ps = rs7.pfgse_sampling(4, pulse_width=0.5, gmax=(0.0, 0.0, 400.0), n_g=8, t_values=[0.4, 1.0, 2.5],
+                            apply_bulk=True, threshold_type="samples", threshold_value=6)
+    out.update({f"pfgse_smp_{k}": v for k, v in ps.items()})
+    del rs7
+
+    # multitau (NMR_multitau::run): log-spaced echo times, one CPMG each, first echo kept
+    rs6 = RefSim(lab, 400, 5, rho=(25.0,), steps_per_echo=3, bulk_time=800.0)
+    mt = rs6.multitau("METHOD: image-based\nOBS_TIME: 12.0\nAPPLY_BULK: true\nSAVE_MODE: false\n",
+                      "TAU_MIN: 0.1\nTAU_MAX: 3.0\nTAU_POINTS: 6\nTAU_SCALE: log\nSAVE_DECAY: true\n")
+    out.update(multitau_steps=mt["steps"], multitau_times=mt["times"], multitau_amps=mt["amps"])
+    del rs6
+
     # walker placement modes (no one-past-the-end pore draws in these cases)
     lab_p = lab.copy()
     nz, ny, nx = lab_p.shape

@@ -107,6 +107,79 @@ def test_cli_sigmoid_relaxivity_matches_reference(tmp_path, golden):
         assert np.all(np.abs(e[:, 2] / e[0, 2] - golden["pfgse_sig_Mkt"][i]) <= 1e-12)
 
 
+@pytest.mark.parametrize("complete", [False, True])
+def test_cli_multitau_matches_reference(tmp_path, golden, complete):
+    """multitau: one CPMG per echo time (log-spaced te, whole even step counts), first echo of each,
+    against the reference's own NMR_multitau run; COMPLETE_DECAY also writes each full decay."""
+    root = str(tmp_path / "config") + "/"
+    write(root + "default/rwnmr.config", RW.format(bulk=800.0, rho=25.0, n=400, spe=3, seed=5))
+    write(root + "default/uct.config", "RESOLUTION: 1.0\nVOXEL_DIVISION: 0\n")
+    write(root + "default/cpmg.config", "METHOD: image-based\nOBS_TIME: 12.0\nAPPLY_BULK: true\nSAVE_MODE: false\n")
+    write(root + "default/multitau.config", "TAU_MIN: 0.1\nTAU_MAX: 3.0\nTAU_POINTS: 6\nTAU_SCALE: log\nSAVE_DECAY: true\n"
+                                            + ("COMPLETE_DECAY: true\n" if complete else ""))
+    assert host.cli(["--config-root", root, "--synthetic", IMG_A, "--quiet", "multitau"], cwd=str(tmp_path)) == 0
+    d = str(tmp_path / "db" / "t") + "//NMR_multitau_min=0.10ms_max=3.00ms_pts=6_scale=log"
+    mt = np.loadtxt(d + "/multitau_decay.csv", delimiter=",", skiprows=1)
+    np.testing.assert_allclose(mt[:, 0], golden["multitau_times"], rtol=1e-15)
+    np.testing.assert_allclose(mt[:, 1], golden["multitau_amps"], rtol=1e-12)
+    te0 = d + "/NMR_cpmg_t=" + ("12.00" if complete else "0.13") + "ms_te=0.133"
+    if complete:
+        decay = np.loadtxt(te0 + "/cpmg_decay.csv", delimiter=",", skiprows=1)
+        assert len(decay) == 91 and decay[1, 1] == mt[0, 1]  # 12 ms / (2 steps x 1/15 ms) echoes + t = 0
+    else:
+        assert os.path.isdir(te0) and not os.path.exists(te0 + "/cpmg_decay.csv")
+
+
+def test_cli_pfgse_walker_sampling_matches_reference(tmp_path, golden):
+    """ALLOW_WALKER_SAMPLING with WALKER_SAMPLES 4: per-sample magnitudes, LHS and least-squares fits,
+    their means and population deviations, per-sample mean squared displacements."""
+    root = str(tmp_path / "config") + "/"
+    write(root + "default/rwnmr.config", RW.format(bulk=900.0, rho=0.0, n=600, spe=1, seed=11) + "WALKER_SAMPLES: 4\n")
+    write(root + "default/uct.config", "RESOLUTION: 1.0\nVOXEL_DIVISION: 0\n")
+    write(root + "default/pfgse.config",
+          "APPLY_BULK: true\nPULSE_WIDTH: 0.5\nMAX_GRADIENT: {0.0, 0.0, 400.0}\nGRADIENT_SAMPLES: 8\n"
+          "TIME_SEQ: manual\nTIME_SAMPLES: 3\nTIME_VALUES: {0.4, 1.0, 2.5}\nAPPLY_SCALE_FACTOR: false\n"
+          "THRESHOLD_TYPE: samples\nTHRESHOLD_VALUE: 6\nALLOW_WALKER_SAMPLING: true\nSAVE_MODE: true\n"
+          "SAVE_PFGSE: true\n")
+    assert host.cli(["--config-root", root, "--synthetic", IMG_A, "--quiet", "pfgse"], cwd=str(tmp_path)) == 0
+    d = str(tmp_path / "db" / "t") + "//NMR_pfgse"
+    res = np.loadtxt(d + "/PFGSE_results.csv", delimiter=",", skiprows=1, ndmin=2)
+    g = {k[len("pfgse_smp_"):]: golden[k] for k in golden if k.startswith("pfgse_smp_")}
+    np.testing.assert_allclose(res[:, 0], g["delta"], rtol=0)
+    np.testing.assert_allclose(res[:, 1], g["dsat"], rtol=1e-10)
+    np.testing.assert_allclose(res[:, 2], g["dsat_err"], rtol=1e-8, atol=1e-15)
+    np.testing.assert_allclose(res[:, 3], g["dsat_std"], rtol=1e-8)
+    assert np.all(res[:, 4] == 6)
+    np.testing.assert_allclose(res[:, 5], g["dmsd"], rtol=1e-12)
+    np.testing.assert_allclose(res[:, 6], g["dmsd_std"], rtol=1e-10)
+    for i in range(3):
+        e = np.loadtxt(d + f"/timesamples/echoes_{i}.csv", delimiter=",", skiprows=1)
+        np.testing.assert_allclose(e[:, 2], g["Mkt"][i], rtol=1e-12)
+        np.testing.assert_allclose(e[:, 4], g["Mstd"][i], rtol=1e-9, atol=1e-12)
+        np.testing.assert_allclose(e[:, 5], g["lhs"][i], rtol=1e-10, atol=1e-13)
+        np.testing.assert_allclose(e[:, 6], g["lhs_std"][i], rtol=1e-8, atol=1e-13)
+
+
+def test_cli_saves_bit_block_image_and_walkers(tmp_path, golden):
+    """SAVE_BINIMG writes NMR_binImage.txt in the reference's layout (fileHandler::writeBitBlockObject3D)
+    with the reference's own bit-blocks; SAVE_WALKERS writes the walkers as created."""
+    root = str(tmp_path / "config") + "/"
+    write(root + "default/rwnmr.config", RW.format(bulk=800.0, rho=25.0, n=400, spe=3, seed=5)
+          + "SAVE_BINIMG: true\nSAVE_WALKERS: true\n")
+    write(root + "default/uct.config", "RESOLUTION: 1.0\nVOXEL_DIVISION: 0\n")
+    assert host.cli(["--config-root", root, "--synthetic", IMG_A, "--quiet"], cwd=str(tmp_path)) == 0
+    lines = open(str(tmp_path / "db" / "t" / "NMR_binImage.txt")).read().split("\n")
+    assert lines[0] == "blocks, bRows, bColumns, bDepth, imgRows, imgColumns, imgDepth, "
+    nb = len(golden["img_a_blocks"])
+    bc, br, bd = (int(v) for v in golden["img_a_bdims"])
+    assert lines[1] == f"{nb}, {br}, {bc}, {bd}, 20, 24, 28" and lines[2] == "" and lines[3] == "blockID, blockData"
+    data = np.array([int(l.split(", ")[1]) for l in lines[4:4 + nb]], np.uint64)
+    assert np.array_equal(data, golden["img_a_blocks"])
+    w = np.loadtxt(str(tmp_path / "db" / "t" / "walkers.csv"), delimiter=",", skiprows=1)
+    assert np.array_equal(w[:, 0], golden["cpmg_x0"]) and np.array_equal(w[:, 5], golden["cpmg_z0"])
+    assert np.all(w[:, 6] == 0) and np.all(w[:, 8] == 1)
+
+
 def test_cli_pfgse_matches_reference_sequence(tmp_path, golden):
     root = str(tmp_path / "config") + "/"
     write(root + "default/rwnmr.config", RW.format(bulk=2800.0, rho=5.0, n=500, spe=1, seed=9))

@@ -86,6 +86,21 @@ def test_missing_user_file_is_an_error(tmp_path):
         config_json("cpmg", str(tmp_path) + "/", str(tmp_path) + "/nope.config")
 
 
+def test_multitau_config_reads_the_cpmg_default_first(tmp_path):
+    """multitau_config's constructor reads default/cpmg.config before the multitau file
+    (multitau_config.cpp:16-22): only its SAVE_* keys carry over; TAU_VALUES are sorted."""
+    root = str(tmp_path) + "/"
+    write(root + "default/cpmg.config", "SAVE_MODE: true\nSAVE_WALKERS: true\nOBS_TIME: 5.0\n")
+    write(root + "default/multitau.config", "TAU_MIN: 0.1\nTAU_MAX: 2.0\nTAU_POINTS: 4\nTAU_SCALE: log\n"
+                                            "SAVE_DECAY: true\n")
+    mt = config_json("multitau", root)
+    assert mt["TAU_SCALE"] == "log" and mt["TAU_POINTS"] == 4 and mt["TAU_MIN"] == 0.1
+    assert mt["SAVE_MODE"] and mt["SAVE_WALKERS"] and mt["SAVE_DECAY"] and not mt["COMPLETE_DECAY"]
+    write(root + "mt.config", "TAU_SCALE: whatever\nTAU_VALUES: {0.5, 0.2, 1.5}\nCOMPLETE_DECAY: True\n")
+    mt2 = config_json("multitau", root, root + "mt.config")
+    assert mt2["TAU_SCALE"] == "manual" and mt2["TAU_VALUES"] == [0.2, 0.5, 1.5] and mt2["COMPLETE_DECAY"]
+
+
 # -- PNG -----------------------------------------------------------------------------------------
 def png_bytes(img, color_type, bit_depth=8, filters=(0,), palette=None):
     """Minimal PNG encoder for the tests (zlib from the standard library)."""
