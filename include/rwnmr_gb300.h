@@ -176,9 +176,11 @@ rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *ctx, const rwnmr_field_cpmg_params 
  * returning. Results equal rwnmr_cpmg_run's (echo_sum to the last bits of FP64 rounding). */
 typedef struct rwnmr_noalloc_cpmg_args
 {
-    const uint64_t *blocks;    /* device: bit-blocks, 1 word per block for one phase; for n_phases
-                                  2 (or 3-4) blocks of 2 (or 4) words: solid mask, then bit-planes
-                                  of the solid voxel's phase index (label - 1) */
+    const uint64_t *blocks;    /* device: bit-blocks, 1 word per block for one phase (the reference's
+                                  array); for n_phases 2 (or 3-4) each block is W = 2 (or 4) words
+                                  -- the solid mask, then bit-planes of the solid voxel's phase index
+                                  (label - 1) -- stored as 2W uint32: the W words' low halves, then
+                                  their high halves */
     int32_t nx, ny, nz, n_phases;
     int64_t n;                 /* walkers */
     const int32_t *x0, *y0, *z0; /* device: initial positions */

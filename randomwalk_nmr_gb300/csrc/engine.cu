@@ -279,6 +279,9 @@ static rwnmr_status set_dims(rwnmr_ctx *c, int32_t nx, int32_t ny, int32_t nz, i
     // engine is the 3D walk, and its noflux reversal needs at least two voxels per axis.
     if (nx < 2 || ny < 2 || nz < 2) return c->fail(RWNMR_ERR_UNSUPPORTED, "3D walks need at least 2 voxels per axis");
     if ((int64_t)nx * ny * nz > (1ll << 40)) return c->fail(RWNMR_ERR_INVALID, "image too large");
+    // the kernels index bit-blocks in 32 bits
+    if ((int64_t)((nx + 3) / 4) * ((ny + 3) / 4) * ((nz + 3) / 4) >= (1ll << 31))
+        return c->fail(RWNMR_ERR_UNSUPPORTED, "images are limited to 2^31 bit-blocks");
     if (n_phases < 1) return c->fail(RWNMR_ERR_INVALID, "n_phases must be >= 1");
     if (n_phases > 4) return c->fail(RWNMR_ERR_UNSUPPORTED, "at most 4 solid phases are supported");
     c->nx = nx;
@@ -326,12 +329,10 @@ rwnmr_status rwnmr_image_upload(rwnmr_ctx *c, const uint64_t *blocks, int32_t nx
         RW_TRY(rwnmr_image_upload_labels(c, labels, nx, ny, nz, n_phases));
         // the labels must describe the same solid voxels as the given bit-blocks
         const int64_t nb = (int64_t)c->bcols * c->brows * c->bdepth;
-        std::vector<uint64_t> packed((size_t)nb * c->words);
-        RW_CUDA(c, cudaMemcpyAsync(packed.data(), c->blocks.p, packed.size() * 8, cudaMemcpyDeviceToHost, c->stream),
-                "blocks readback");
-        RW_CUDA(c, cudaStreamSynchronize(c->stream), "blocks readback");
+        std::vector<uint64_t> packed((size_t)nb);
+        RW_TRY(rwnmr_image_download_blocks(c, packed.data()));
         for (int64_t b = 0; b < nb; b++)
-            if (packed[(size_t)b * c->words] != blocks[b])
+            if (packed[(size_t)b] != blocks[b])
             {
                 c->has_image = false;
                 return c->fail(RWNMR_ERR_INVALID, "labels disagree with bit-block %lld", (long long)b);
@@ -358,13 +359,19 @@ rwnmr_status rwnmr_image_download_blocks(rwnmr_ctx *c, uint64_t *out)
     if (c->words == 1)
     {
         RW_CUDA(c, cudaMemcpyAsync(out, c->blocks.p, (size_t)nb * 8, cudaMemcpyDeviceToHost, c->stream), "blocks download");
+        RW_CUDA(c, cudaStreamSynchronize(c->stream), "blocks download");
+        return RWNMR_OK;
     }
-    else
-    {
-        RW_CUDA(c, cudaMemcpy2DAsync(out, 8, c->blocks.p, (size_t)8 * c->words, 8, (size_t)nb, cudaMemcpyDeviceToHost,
-                                     c->stream), "blocks download");
-    }
+    // multi-phase blocks: the solid word's halves sit at uint32 2W*b and 2W*b + W
+    const int W = c->words;
+    std::vector<uint32_t> lo((size_t)nb), hi((size_t)nb);
+    const uint32_t *dev = reinterpret_cast<const uint32_t *>(c->blocks.p);
+    RW_CUDA(c, cudaMemcpy2DAsync(lo.data(), 4, dev, (size_t)8 * W, 4, (size_t)nb, cudaMemcpyDeviceToHost, c->stream),
+            "blocks download");
+    RW_CUDA(c, cudaMemcpy2DAsync(hi.data(), 4, dev + W, (size_t)8 * W, 4, (size_t)nb, cudaMemcpyDeviceToHost, c->stream),
+            "blocks download");
     RW_CUDA(c, cudaStreamSynchronize(c->stream), "blocks download");
+    for (int64_t b = 0; b < nb; b++) out[b] = (uint64_t)lo[(size_t)b] | ((uint64_t)hi[(size_t)b] << 32);
     return RWNMR_OK;
 }
 

@@ -116,6 +116,8 @@ extern "C" rwnmr_status rwnmr_cpmg_run_noalloc(const rwnmr_cpmg_params *p, const
         return say(err, errlen, RWNMR_ERR_INVALID, "bad boundary condition or voxel-division shift");
     if (p->n_echoes < 0 || p->steps_per_echo < 1) return say(err, errlen, RWNMR_ERR_INVALID, "bad echo count / steps per echo");
     if (a->nx < 2 || a->ny < 2 || a->nz < 2) return say(err, errlen, RWNMR_ERR_UNSUPPORTED, "3D walks need at least 2 voxels per axis");
+    if ((int64_t)((a->nx + 3) / 4) * ((a->ny + 3) / 4) * ((a->nz + 3) / 4) >= (1ll << 31))
+        return say(err, errlen, RWNMR_ERR_UNSUPPORTED, "images are limited to 2^31 bit-blocks");
     if (a->n_phases < 1 || a->n_phases > 4) return say(err, errlen, RWNMR_ERR_UNSUPPORTED, "1 to 4 solid phases are supported");
     if (a->n < 0 || a->n > (1ll << 31) - 1) return say(err, errlen, RWNMR_ERR_INVALID, "walker count out of range");
     if (!p->dfactor) return say(err, errlen, RWNMR_ERR_INVALID, "dfactor is NULL");

@@ -27,8 +27,12 @@ enum
     BC_GENERIC = 3 // any bc with voxel division: runtime bc, reference formulas
 };
 
-// Bit-block image on the device. Each block holds W consecutive 64-bit words: word 0 is the solid
-// mask, words 1..W-1 are bit-planes of the solid voxel's phase index (multi-phase images only).
+// Bit-block image on the device, read as 32-bit halves: block b occupies 2W uint32 at 2W*b, half h
+// (bits 32h..32h+31 of the 4x4x4 block) at 2W*b + W*h, as W words: the solid mask, then (multi-
+// phase images, W = 2 or 4) bit-planes of the solid voxel's phase index. For W = 1 this is the
+// reference's uint64 block array itself (little-endian halves); for W > 1 one aligned 8- or
+// 16-byte load returns the solid bit and the phase bits of a voxel. Blocks are indexed in 32 bits
+// (images of fewer than 2^31 blocks, checked on the host).
 struct DevImage
 {
     const uint64_t *__restrict__ blocks;
@@ -161,13 +165,14 @@ __device__ __forceinline__ void current_voxel(const DevImage &im, const WalkerPo
     }
 }
 
-// Solid bit of an image voxel (word 0 of its block).
+// Solid bit of an image voxel (solid word of its block half).
 template <int W>
 __device__ __forceinline__ bool voxel_solid(const DevImage &im, int ix, int iy, int iz)
 {
-    const int64_t blk = (int64_t)(ix >> 2) + (int64_t)(iy >> 2) * im.bcols + (int64_t)(iz >> 2) * im.bcr;
+    const uint32_t blk = (uint32_t)(ix >> 2) + (uint32_t)(iy >> 2) * (uint32_t)im.bcols + (uint32_t)(iz >> 2) * (uint32_t)im.bcr;
     const uint32_t bit = (uint32_t)((ix & 3) | ((iy & 3) << 2) | ((iz & 3) << 4));
-    return ((__ldg(im.blocks + blk * W) >> bit) & 1ull) != 0;
+    const uint32_t *bp = reinterpret_cast<const uint32_t *>(im.blocks) + (size_t)blk * (2 * W) + (bit >> 5) * W;
+    return ((__ldg(bp) >> (bit & 31u)) & 1u) != 0;
 }
 
 // Returns true if a walker may start at p: inside the image for noflux (in walk units).
@@ -270,10 +275,11 @@ __device__ __forceinline__ void walker_step(const DevImage &im, WalkerPos &p, ui
         }
     }
 
-    const int64_t blk = (int64_t)(cix >> 2) + (int64_t)(ciy >> 2) * im.bcols + (int64_t)(ciz >> 2) * im.bcr;
+    const uint32_t blk = (uint32_t)(cix >> 2) + (uint32_t)(ciy >> 2) * (uint32_t)im.bcols + (uint32_t)(ciz >> 2) * (uint32_t)im.bcr;
     const uint32_t bit = (uint32_t)((cix & 3) | ((ciy & 3) << 2) | ((ciz & 3) << 4));
-    const uint64_t *bp = im.blocks + blk * W;
-    uint64_t solid;
+    const uint32_t sh = bit & 31u;
+    const uint32_t *bp = reinterpret_cast<const uint32_t *>(im.blocks) + (size_t)blk * (2 * W) + (bit >> 5) * W;
+    uint32_t solid;
     phase = 0;
     if (W == 1)
     {
@@ -281,18 +287,17 @@ __device__ __forceinline__ void walker_step(const DevImage &im, WalkerPos &p, ui
     }
     else if (W == 2)
     {
-        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(bp));
+        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(bp));
         solid = v.x;
-        phase = (int)((v.y >> bit) & 1ull);
+        phase = (int)((v.y >> sh) & 1u);
     }
     else
     {
-        ulonglong2 v0 = __ldg(reinterpret_cast<const ulonglong2 *>(bp));
-        ulonglong2 v1 = __ldg(reinterpret_cast<const ulonglong2 *>(bp) + 1);
-        solid = v0.x;
-        phase = (int)(((v0.y >> bit) & 1ull) | (((v1.x >> bit) & 1ull) << 1) | (((v1.y >> bit) & 1ull) << 2));
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(bp));
+        solid = v.x;
+        phase = (int)(((v.y >> sh) & 1u) | (((v.z >> sh) & 1u) << 1) | (((v.w >> sh) & 1u) << 2));
     }
-    wall = ((solid >> bit) & 1ull) != 0;
+    wall = ((solid >> sh) & 1u) != 0;
     if (!wall)
     {
         p.x = tx;

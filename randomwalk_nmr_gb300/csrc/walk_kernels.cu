@@ -53,8 +53,18 @@ __device__ __forceinline__ void load_pos(const WalkState &s, int64_t i, WalkerPo
 // Walker::decreaseFactor, e.g. from a sigmoid of its collision rate) and its energy is the FP64
 // repeated product f_w * f_w * ..., one multiply per collision as in Walker::walk_3D, applied after
 // each echo for the collisions the echo gained and rounded to the same 2^63 fixed point.
+// Occupancy: at 256 threads, 8 resident blocks per SM need <= 32 registers a thread, 6 need <= 40,
+// 5 need <= 48. The minimum-block bounds below were chosen by measurement (+4 % two-phase, +6 %
+// one-phase walker-steps/s over the unbounded build); a few instances spill up to 16 bytes.
 template <int BC, int NP, bool PACK, bool WF>
-__global__ void __launch_bounds__(kWalkThreads) cpmg_walk_kernel(DevImage im, WalkState st, CpmgLaunch L)
+constexpr int cpmg_min_blocks()
+{
+    return NP == 4 ? 5 : ((BC == BC_NOFLUX || BC == BC_GENERIC) && !WF && (NP == 1 || PACK) ? 8 : 6);
+}
+
+template <int BC, int NP, bool PACK, bool WF>
+__global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, WF>()))
+    cpmg_walk_kernel(DevImage im, WalkState st, CpmgLaunch L)
 {
     static_assert(!PACK || NP == 2, "packed collision counts are for two phases");
     static_assert(!WF || NP == 1, "per-walker decrease factors are for single-phase images");
@@ -559,14 +569,11 @@ __global__ void pack_blocks_kernel(const uint8_t *__restrict__ labels, int nx, i
         p1 |= (uint64_t)((ph >> 1) & 1u) << k;
         p2 |= (uint64_t)((ph >> 2) & 1u) << k;
     }
-    uint64_t *o = out + b * words;
-    o[0] = solid;
-    if (words >= 2) o[1] = p0;
-    if (words >= 4)
-    {
-        o[2] = p1;
-        o[3] = p2;
-    }
+    // half-interleaved layout (see DevImage): the words' low halves, then their high halves
+    uint32_t *o = reinterpret_cast<uint32_t *>(out) + b * 2 * words;
+    const uint64_t wv[4] = {solid, p0, p1, p2};
+    for (int h = 0; h < 2; h++)
+        for (int w = 0; w < words; w++) o[h * words + w] = (uint32_t)(wv[w] >> (32 * h));
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -206,3 +206,25 @@ def test_cpmg_per_walker_dfactor_equal_factors_match_tables(engine):
     engine.set_walker_dfactor(np.full(len(w[0]), f))
     with pytest.raises(RwnmrError, match="single-phase"):
         engine.cpmg(10, 2, None)
+
+
+@pytest.mark.parametrize("n_phases", [1, 2, 3])
+def test_image_upload_and_download_blocks(engine, golden, n_phases):
+    """GPU packing of labels (with phase planes) returns the reference's bit-blocks as solid masks;
+    blocks + labels are accepted when they agree and rejected when they do not."""
+    from randomwalk_nmr_gb300 import RwnmrError
+
+    lab = golden["img_a"].astype(np.uint8)
+    if n_phases > 1:
+        lab = image(shape=lab.shape, n_phases=n_phases, seed=17)
+    blocks, _ = host.pack_blocks(lab)
+    engine.upload_labels(lab, n_phases)
+    assert np.array_equal(engine.download_blocks(), blocks)
+    if n_phases == 1:
+        assert np.array_equal(blocks, golden["img_a_blocks"])
+    engine.upload_blocks(blocks, lab.shape, lab if n_phases > 1 else None, n_phases)
+    assert np.array_equal(engine.download_blocks(), blocks)
+    bad = blocks.copy()
+    bad[len(bad) // 2] ^= np.uint64(1)
+    with pytest.raises(RwnmrError, match="disagree"):
+        engine.upload_blocks(bad, lab.shape, lab, n_phases)

@@ -47,7 +47,9 @@ def device_blocks(labels, n_phases):
         vals = np.zeros(len(blocks), np.uint64)
         np.bitwise_or.at(vals, blk[sel], np.left_shift(np.uint64(1), bit[sel].astype(np.uint64)))
         out[:, plane + 1] = vals
-    return out.reshape(-1)
+    # each block as 2W uint32: the W words' low halves, then their high halves
+    halves = np.concatenate([out & np.uint64(0xFFFFFFFF), out >> np.uint64(32)], axis=1).astype(np.uint32)
+    return halves.reshape(-1).view(np.uint64)
 
 
 @pytest.mark.parametrize("n_phases", [1, 2])
