@@ -13,7 +13,7 @@ Reported:
   e2e        the same metric through the C ABI from pinned host buffers: image labels and walker
              initial state copied host->device, echo train and per-echo collisions copied back
   roofline   achieved gather bytes of the dominant kernel against the measured HBM copy peak, plus
-             the integer-issue bound (see the design doc for the algorithmic figures)
+             the integer-issue bound (warp-instructions per walker-step from an ncu capture)
   cpu_baseline  the oracle's CPU walk (port of the reference's Walker::walk) on a bounded walker
              sample with all host threads
 
@@ -204,7 +204,7 @@ def _sphere_image(args):
 
 
 def run_fit_multiphase(args):
-    """Differentiable CPMG fit (BASELINE configs[3]): 200^3, 4 solid phases, 500k walkers, 5000 echoes
+    """Differentiable CPMG fit of a multi-phase image: 200^3, 4 solid phases, 500k walkers, 5000 echoes
     of 3 steps; L-BFGS with adjoint gradients vs the restated GA (population 64) on the same GPU walk."""
     import torch
 
@@ -254,7 +254,7 @@ def run_fit_multiphase(args):
 
 
 def run_fit_batch(args):
-    """Batched uneven workload (BASELINE configs[4]): 64 sphere packs with edges U[64, 320], walkers
+    """Batched uneven workload: 64 sphere packs with edges U[64, 320], walkers
     U[1e4, 5e5], 16 relaxivity candidates per image, 3000 echoes of 3 steps, one persistent launch per
     fit iteration (CUDA graph, autotuned block size), vs per-image plain CPMG + the restated GA."""
     from concurrent.futures import ThreadPoolExecutor
@@ -427,8 +427,8 @@ def main():
                "d2h_bytes_per_step": int(d2h), "ms_per_step": te * 1e3}
 
     peak, peak_kind, peaks = measured_peaks()
-    words = 1 if w["n_phases"] == 1 else 2
-    gather_bytes = 8 * words  # algorithmic bytes gathered per walker-step (bit-block words)
+    words = 1 if w["n_phases"] == 1 else (2 if w["n_phases"] == 2 else 4)
+    gather_bytes = 4 * words  # algorithmic bytes gathered per walker-step: one 32-bit half of each block word
     launches_per_walk = max(1, launches // max(1, args.steps))
     achieved = steps_per_run * gather_bytes / t_step / 1e9
     counters = {}
@@ -444,7 +444,7 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": counters.get("dram_bytes_per_launch"), "traffic_unit": "bytes per launch",
                 "launches_per_walk": launches_per_walk, "peak_source": peak_kind,
-                "note": ("achieved = bit-block bytes gathered per walker-step (8 B per word) x walker-steps / "
+                "note": ("achieved = bit-block bytes gathered per walker-step (4 B per block word) x walker-steps / "
                          "walk-kernel time, against the measured HBM copy peak; the gathers are L2-served "
                          "(ncu: 93% L2 hit, 33 MB DRAM per launch), so the binding roof is instruction issue, "
                          "reported under 'issue'")}
