@@ -361,6 +361,35 @@ def run_pfgse(args):
     from randomwalk_nmr_gb300 import Engine
 
     w, res, steps, kvec, f, deltas = pfgse_setup(args.workload.endswith("-small"))
+    if args.impl == "reference":
+        # reference arm: the reference's CPU PFGSE walk and phase sums (oracle port) on a bounded sample
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        from oracle.pyoracle import Oracle, build
+
+        labels, por, walkers = build_inputs(w)
+        build(with_ref=False)
+        o = Oracle()
+        threads = os.cpu_count() or 1
+        m = min(len(walkers[0]), 64 * 1024)
+        sample = tuple(a[:m] for a in walkers)
+        for _ in range(args.warmup):
+            o.pfgse(labels, sample, f, steps[:3], kvec, res, threads=threads)
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            o.pfgse(labels, sample, f, steps, kvec, res, threads=threads)
+            ts.append(time.perf_counter() - t0)
+        v = m * int(steps[-1]) / statistics.mean(ts)
+        print(json.dumps({"impl": "reference", "metric": "walker-steps/s (PFGSE)", "value": v, "unit": "walker-steps/s",
+                          "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": statistics.mean(ts) * 1e3, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "data": "synthetic sphere pack",
+                          "config": {"workload": w["name"], "walkers_sampled": m},
+                          "cpu_baseline": {"value": v, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+                                           "sample": f"first {m} walkers, all 10 exposure times"},
+                          "e2e": {"value": v, "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     labels, por, walkers = build_inputs(w)
