@@ -70,6 +70,24 @@ def test_pfgse_multiphase(engine, oracle):
     assert np.all(np.abs(g["M"] - o["M"]) <= ATT_TOL * o["M"][:, :1])
 
 
+@pytest.mark.parametrize("bc", ["noflux", "periodic", "mirror"])
+def test_pfgse_voxel_division(engine, oracle, bc):
+    """Voxel division (walk grid 2x finer than the image): axis and oblique gradients."""
+    lab, _ = host.synth_spheres((24, 22, 26), 2.0, 6.0, 0.4, 1, seed=12)
+    blocks, _ = host.pack_blocks(lab)
+    w = host.place_walkers(blocks, lab.shape, 3000, 77, "random", 0, 1)[:4]
+    engine.upload_labels(lab, 1)
+    engine.upload_walkers(*w)
+    steps = np.array([30, 80, 200], np.int32)
+    f = dfactor(15.0, res=0.5)
+    for gdir in ((0, 0, 150.0), (40.0, 30.0, 60.0)):
+        kv = kvecs(12, gdir)
+        g = engine.pfgse(steps, kv, 0.5, f, bc=bc, shift=1)
+        o = oracle.pfgse(lab, w, f, steps, kv, 0.5, bc=bc, shift=1, threads=4)
+        assert np.array_equal(g["msd"], o["msd"])
+        assert np.all(np.abs(g["M"] - o["M"]) <= ATT_TOL * o["M"][:, :1])
+
+
 @pytest.mark.parametrize("gdir", [(0, 0, 1.0), (0.6, 0.0, 0.8)])
 def test_pfgse_grad_g_matches_finite_differences(engine, gdir):
     lab, w = setup(engine, seed=5)
