@@ -62,7 +62,8 @@ constexpr int cpmg_min_blocks()
     return NP == 4 ? 5 : ((BC == BC_NOFLUX || BC == BC_GENERIC) && !WF && (NP == 1 || PACK) ? 8 : 6);
 }
 
-template <int BC, int NP, bool PACK, bool WF>
+// ONE: one step per echo (the common fine-time-step case), the step loop compiled away.
+template <int BC, int NP, bool PACK, bool WF, bool ONE>
 __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, WF>()))
     cpmg_walk_kernel(DevImage im, WalkState st, CpmgLaunch L)
 {
@@ -145,7 +146,8 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
             for (int k = 0; k < NG; k++) g[k] = 0;
             if (active)
             {
-                for (int s = 0; s < L.steps_per_echo; s++)
+                const int spe = ONE ? 1 : L.steps_per_echo;
+                for (int s = 0; s < spe; s++)
                 {
                     bool wall;
                     int ph;
@@ -602,17 +604,22 @@ cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkS
             constexpr int BC = decltype(bcc)::value;
             // packed counts: a lane's half-word holds at most steps_per_echo < 2^16 collisions, and a
             // recorded echo's warp sum of a half at most 32 * steps_per_echo < 2^16
-            if constexpr (NP == 1)
-            {
-                if (L.wf)
-                    cpmg_walk_kernel<BC, 1, false, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            auto run = [&](auto one) {
+                constexpr bool ONE = decltype(one)::value;
+                if constexpr (NP == 1)
+                {
+                    if (L.wf)
+                        cpmg_walk_kernel<BC, 1, false, true, ONE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    else
+                        cpmg_walk_kernel<BC, 1, false, false, ONE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                }
+                else if (NP == 2 && L.steps_per_echo <= (L.record ? 2047 : 65535))
+                    cpmg_walk_kernel<BC, NP, NP == 2, false, ONE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
                 else
-                    cpmg_walk_kernel<BC, 1, false, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
-            }
-            else if (NP == 2 && L.steps_per_echo <= (L.record ? 2047 : 65535))
-                cpmg_walk_kernel<BC, NP, NP == 2, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
-            else
-                cpmg_walk_kernel<BC, NP, false, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    cpmg_walk_kernel<BC, NP, false, false, ONE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            };
+            if (L.record && L.steps_per_echo == 1) run(std::true_type{});
+            else run(std::false_type{});
         });
     };
     if (np == 1) go(std::integral_constant<int, 1>{});
