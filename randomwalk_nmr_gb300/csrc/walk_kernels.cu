@@ -62,8 +62,9 @@ constexpr int cpmg_min_blocks()
     return NP == 4 ? 5 : ((BC == BC_NOFLUX || BC == BC_GENERIC) && !WF && (NP == 1 || PACK) ? 8 : 6);
 }
 
-// ONE: one step per echo (the common fine-time-step case), the step loop compiled away.
-template <int BC, int NP, bool PACK, bool WF, bool ONE>
+// SPE: steps per echo known at compile time (1, 2 or 3, the common cases; 0 = read from the launch),
+// so the step loop unrolls away.
+template <int BC, int NP, bool PACK, bool WF, int SPE>
 __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, WF>()))
     cpmg_walk_kernel(DevImage im, WalkState st, CpmgLaunch L)
 {
@@ -146,7 +147,8 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
             for (int k = 0; k < NG; k++) g[k] = 0;
             if (active)
             {
-                const int spe = ONE ? 1 : L.steps_per_echo;
+                const int spe = SPE ? SPE : L.steps_per_echo;
+#pragma unroll
                 for (int s = 0; s < spe; s++)
                 {
                     bool wall;
@@ -604,22 +606,25 @@ cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkS
             constexpr int BC = decltype(bcc)::value;
             // packed counts: a lane's half-word holds at most steps_per_echo < 2^16 collisions, and a
             // recorded echo's warp sum of a half at most 32 * steps_per_echo < 2^16
-            auto run = [&](auto one) {
-                constexpr bool ONE = decltype(one)::value;
+            auto run = [&](auto spe) {
+                constexpr int SPE = decltype(spe)::value;
                 if constexpr (NP == 1)
                 {
                     if (L.wf)
-                        cpmg_walk_kernel<BC, 1, false, true, ONE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                        cpmg_walk_kernel<BC, 1, false, true, SPE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
                     else
-                        cpmg_walk_kernel<BC, 1, false, false, ONE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                        cpmg_walk_kernel<BC, 1, false, false, SPE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
                 }
                 else if (NP == 2 && L.steps_per_echo <= (L.record ? 2047 : 65535))
-                    cpmg_walk_kernel<BC, NP, NP == 2, false, ONE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    cpmg_walk_kernel<BC, NP, NP == 2, false, SPE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
                 else
-                    cpmg_walk_kernel<BC, NP, false, false, ONE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    cpmg_walk_kernel<BC, NP, false, false, SPE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
             };
-            if (L.record && L.steps_per_echo == 1) run(std::true_type{});
-            else run(std::false_type{});
+            const int spe = L.record ? L.steps_per_echo : 0;
+            if (spe == 1) run(std::integral_constant<int, 1>{});
+            else if (spe == 2) run(std::integral_constant<int, 2>{});
+            else if (spe == 3) run(std::integral_constant<int, 3>{});
+            else run(std::integral_constant<int, 0>{});
         });
     };
     if (np == 1) go(std::integral_constant<int, 1>{});
