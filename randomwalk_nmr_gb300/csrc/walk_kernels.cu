@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
             if (active)
             {
                 const int spe = SPE ? SPE : L.steps_per_echo;
-#pragma unroll
+#pragma unroll(SPE ? SPE : 4)
                 for (int s = 0; s < spe; s++)
                 {
                     bool wall;
@@ -385,6 +385,7 @@ __global__ void __launch_bounds__(kWalkThreads) pfgse_walk_kernel(DevImage im, W
         const int target = L.steps[d];
         if (active)
         {
+#pragma unroll 4
             for (; done < target; done++)
             {
                 bool wall;
