@@ -216,6 +216,8 @@ typedef struct rwnmr_batch_cpmg_params
     int32_t derivatives;       /* also return dM/df per candidate */
     int32_t threads_per_block; /* 0 = autotuned value (or 256 before rwnmr_batch_autotune) */
     int32_t use_graph;         /* replay the launch sequence as a captured CUDA graph */
+    int32_t walkers_per_thread; /* 1 or 2; 0 = autotuned value (or 1 before rwnmr_batch_autotune).
+                                   Results do not depend on it (exact integer sums). */
 } rwnmr_batch_cpmg_params;
 
 rwnmr_status rwnmr_batch_create(rwnmr_batch **out, int device);
@@ -230,9 +232,10 @@ rwnmr_status rwnmr_batch_add_image(rwnmr_batch *batch, const uint64_t *blocks, i
 /* dfactor [n_images][n_candidates]; echo and decho (nullable) [n_images][n_candidates][n_echoes+1]. */
 rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *batch, const rwnmr_batch_cpmg_params *p, const double *dfactor,
                               double *echo, double *decho);
-/* Times the walk for 128, 256 and 512 threads per block and keeps the fastest for later calls. */
+/* Times the walk for 128, 256 and 512 threads per block with 1 and 2 walkers per thread and keeps
+ * the fastest pair for later calls (outputs nullable). */
 rwnmr_status rwnmr_batch_autotune(rwnmr_batch *batch, const rwnmr_batch_cpmg_params *p, int32_t *best_threads,
-                                  double *best_ms);
+                                  int32_t *best_walkers_per_thread, double *best_ms);
 
 /* ---- collision-mapping walk ------------------------------------------------------------ */
 /* NMR_Simulation::mapSimulation (NMR_Simulation.cpp:1787-1841; NMR_Simulation_cuda.cpp:726-1270):

@@ -15,7 +15,8 @@
 //
 // The sequence table kernel -> accumulator reset -> walk -> copy-out is captured once in a CUDA
 // graph and replayed for every new set of candidates (a fit iteration changes only the pinned
-// decrease-factor buffer). The block size is chosen by a short timed sweep (rwnmr_batch_autotune).
+// decrease-factor buffer). The block size and the walkers per thread (1 or 2: two walkers share one
+// transpose) are chosen by a short timed sweep (rwnmr_batch_autotune).
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -37,7 +38,8 @@ namespace
 {
 constexpr int kCand = 16;             // candidate slots per image
 constexpr int kWin = 16;              // echoes per shared-memory window
-constexpr double kEScale = 288230376151711744.0; // 2^58: energy scale (32 lanes sum below 2^63)
+constexpr double kEScale = 144115188075855872.0; // 2^57: energy scale (2 walkers x 32 lanes sum below 2^63)
+constexpr int kScaleBits = 57;
 constexpr unsigned FULLM = 0xffffffffu;
 
 struct BatchImage
@@ -65,7 +67,8 @@ struct BatchLaunch
     int32_t n_echoes, steps_per_echo, bc;
     int32_t deriv;
     int32_t tstride;             // entries per candidate table (n_echoes * steps_per_echo + 1)
-    const unsigned long long *tab; // [image][cand][2][tstride]: energy, derivative
+    int32_t dshift;              // derivative c f^(c-1) = c * (T[c-1] >> dshift), scale 2^(57 - dshift)
+    const unsigned long long *tab; // [image][cand][tstride]: energy round(f^c 2^57)
     unsigned long long *acc;       // [image][n_echoes + 1][cand][4]: energy lo/hi, derivative lo/hi
     const int32_t *x0, *y0, *z0;
     const uint64_t *seed0;
@@ -95,8 +98,10 @@ __device__ __forceinline__ unsigned long long transpose_reduce16(unsigned long l
     return v[0] + __shfl_xor_sync(FULLM, v[0], 1);
 }
 
-template <int BC>
-__global__ void __launch_bounds__(512) batch_cpmg_kernel(BatchLaunch L)
+// WPT walkers per thread: the thread walks walkers first + threadIdx.x + j * blockDim.x, j < WPT,
+// and adds their table values before the warp transpose, so one transpose serves 32 * WPT walkers.
+template <int BC, int WPT>
+__global__ void __launch_bounds__(512, 2) batch_cpmg_kernel(BatchLaunch L)
 {
     extern __shared__ unsigned long long sacc[]; // [kWin][kCand][4]
     __shared__ int s_item;
@@ -119,26 +124,34 @@ __global__ void __launch_bounds__(512) batch_cpmg_kernel(BatchLaunch L)
         im.bcr = img.bcr;
         im.bc = L.bc;
         im.shift = 0;
-        const int64_t i = w.first + threadIdx.x;
-        bool active = i < w.last;
-        WalkerPos p{};
-        uint64_t seed = 0;
-        if (active)
+        WalkerPos p[WPT];
+        uint64_t seed[WPT];
+        bool active[WPT];
+        uint32_t c[WPT];
+#pragma unroll
+        for (int j = 0; j < WPT; j++)
         {
-            p.x = L.x0[i];
-            p.y = L.y0[i];
-            p.z = L.z0[i];
-            seed = L.seed0[i];
-            if (!start_ok<BC>(im, p))
+            p[j] = WalkerPos{};
+            seed[j] = 0;
+            c[j] = 0;
+            const int64_t i = w.first + threadIdx.x + (int64_t)j * blockDim.x;
+            active[j] = i < w.last;
+            if (active[j])
             {
-                atomicOr(L.status, kStatusBadStart);
-                active = false;
+                p[j].x = L.x0[i];
+                p[j].y = L.y0[i];
+                p[j].z = L.z0[i];
+                seed[j] = L.seed0[i];
+                if (!start_ok<BC>(im, p[j]))
+                {
+                    atomicOr(L.status, kStatusBadStart);
+                    active[j] = false;
+                }
+                init_image_coords<BC>(im, p[j]);
             }
-            init_image_coords<BC>(im, p);
         }
         const unsigned long long *tabE = L.tab + img.tab0;
         unsigned long long *acc = L.acc + img.acc0;
-        uint32_t c = 0;
         for (int k = threadIdx.x; k < kWin * kCand * 4; k += blockDim.x) sacc[k] = 0;
         __syncthreads();
         for (int e0 = -1; e0 < L.n_echoes; e0 += kWin)
@@ -147,18 +160,25 @@ __global__ void __launch_bounds__(512) batch_cpmg_kernel(BatchLaunch L)
             const int e1 = min(e0 + kWin, L.n_echoes);
             for (int e = e0 + 1; e <= e1; e++)
             {
-                if (active && e > 0)
-                    for (int s = 0; s < L.steps_per_echo; s++)
-                    {
-                        bool wall;
-                        int ph;
-                        walker_step<BC, 1>(im, p, seed, wall, ph);
-                        c += wall ? 1u : 0u;
-                    }
+#pragma unroll
+                for (int j = 0; j < WPT; j++)
+                    if (active[j] && e > 0)
+                        for (int s = 0; s < L.steps_per_echo; s++)
+                        {
+                            bool wall;
+                            int ph;
+                            walker_step<BC, 1>(im, p[j], seed[j], wall, ph);
+                            c[j] += wall ? 1u : 0u;
+                        }
                 unsigned long long v[kCand];
 #pragma unroll
                 for (int r = 0; r < kCand; r++)
-                    v[r] = active ? __ldg(tabE + ((size_t)r * 2) * L.tstride + c) : 0ull;
+                {
+                    v[r] = 0;
+#pragma unroll
+                    for (int j = 0; j < WPT; j++)
+                        v[r] += active[j] ? __ldg(tabE + (size_t)r * L.tstride + c[j]) : 0ull;
+                }
                 const unsigned long long sumE = transpose_reduce16(v, lane);
                 const int slot = e - (e0 + 1);
                 // a warp sum is below 2^63; its 32-bit halves accumulate without overflow
@@ -172,7 +192,12 @@ __global__ void __launch_bounds__(512) batch_cpmg_kernel(BatchLaunch L)
                 {
 #pragma unroll
                     for (int r = 0; r < kCand; r++)
-                        v[r] = active ? __ldg(tabE + ((size_t)r * 2 + 1) * L.tstride + c) : 0ull;
+                    {
+                        v[r] = 0;
+#pragma unroll
+                        for (int j = 0; j < WPT; j++)
+                            v[r] += (active[j] && c[j]) ? (unsigned long long)c[j] * (__ldg(tabE + (size_t)r * L.tstride + c[j] - 1) >> L.dshift) : 0ull;
+                    }
                     const unsigned long long sumU = transpose_reduce16(v, lane);
                     if ((lane & 1) == 0)
                     {
@@ -194,26 +219,37 @@ __global__ void __launch_bounds__(512) batch_cpmg_kernel(BatchLaunch L)
     }
 }
 
-// Tables for every (image, candidate): energy round(f^c 2^58) and derivative round(c f^(c-1) 2^us),
-// f^c the FP64 repeated product. One thread per (image, candidate).
-__global__ void batch_tables_kernel(const double *__restrict__ f, int n_images, const int32_t *__restrict__ ushift,
-                                    int tstride, unsigned long long *__restrict__ tab)
+// Energy tables for every (image, candidate): round(f^c 2^57), f^c the FP64 repeated product. The
+// walk derives the derivative c f^(c-1) from the same table (c * (T[c-1] >> dshift), exact integer
+// arithmetic), so only one table per candidate competes for L2. One thread per (image, candidate).
+__global__ void batch_tables_kernel(const double *__restrict__ f, int n_images, int tstride,
+                                    unsigned long long *__restrict__ tab)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_images * kCand) return;
-    const int img = t / kCand;
     const double fr = f[t];
-    const double us = ldexp(1.0, ushift[img]);
-    unsigned long long *te = tab + ((size_t)t * 2) * tstride;
-    unsigned long long *tu = te + tstride;
-    double v = 1.0, prev = 0.0;
+    unsigned long long *te = tab + (size_t)t * tstride;
+    double v = 1.0;
     for (int k = 0; k < tstride; k++)
     {
         te[k] = __double2ull_rn(v * kEScale);
-        tu[k] = k == 0 ? 0ull : __double2ull_rn((double)k * prev * us);
-        prev = v;
         v = v * fr;
     }
+}
+
+// Interleaves the low 21 bits of x, y, z (Morton / Z-order key).
+uint64_t morton3(uint32_t x, uint32_t y, uint32_t z)
+{
+    auto spread = [](uint64_t v) {
+        v &= 0x1fffff;
+        v = (v | v << 32) & 0x1f00000000ffffull;
+        v = (v | v << 16) & 0x1f0000ff0000ffull;
+        v = (v | v << 8) & 0x100f00f00f00f00full;
+        v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+        v = (v | v << 2) & 0x1249249249249249ull;
+        return v;
+    };
+    return spread(x) | (spread(y) << 1) | (spread(z) << 2);
 }
 
 rwnmr_status put(std::string &s, rwnmr_status st, const char *fmt, ...)
@@ -243,13 +279,13 @@ struct rwnmr_batch
     uint64_t *d_blocks = nullptr;
     BatchImage *d_images = nullptr;
     WorkItem *d_items = nullptr;
-    int32_t *d_x = nullptr, *d_y = nullptr, *d_z = nullptr, *d_ushift = nullptr;
+    int32_t *d_x = nullptr, *d_y = nullptr, *d_z = nullptr;
     uint64_t *d_seed = nullptr;
     unsigned long long *d_tab = nullptr, *d_acc = nullptr;
     unsigned *d_counter = nullptr, *d_status = nullptr;
     double *d_f = nullptr;
     size_t tab_words = 0, acc_words = 0;
-    int n_items = 0, items_block = 0;
+    int n_items = 0, items_block = 0; // items_block: walkers per work item
     // pinned host staging and the captured graph
     double *h_f = nullptr;
     unsigned long long *h_acc = nullptr;
@@ -259,7 +295,7 @@ struct rwnmr_batch
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0.0;
     int64_t launches = 0;
-    int tuned_block = 0;
+    int tuned_block = 0, tuned_wpt = 0;
     int sms = 0;
 
     void free_device()
@@ -267,13 +303,13 @@ struct rwnmr_batch
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
         for (void *p : {(void *)d_blocks, (void *)d_images, (void *)d_items, (void *)d_x, (void *)d_y, (void *)d_z,
-                        (void *)d_ushift, (void *)d_seed, (void *)d_tab, (void *)d_acc, (void *)d_counter,
+                        (void *)d_seed, (void *)d_tab, (void *)d_acc, (void *)d_counter,
                         (void *)d_status, (void *)d_f})
             if (p) cudaFree(p);
         d_blocks = nullptr;
         d_images = nullptr;
         d_items = nullptr;
-        d_x = d_y = d_z = d_ushift = nullptr;
+        d_x = d_y = d_z = nullptr;
         d_seed = nullptr;
         d_tab = d_acc = nullptr;
         d_counter = d_status = nullptr;
@@ -304,7 +340,7 @@ rwnmr_status upload(rwnmr_batch *b, int n_echoes, int spe)
     const int64_t nmax = (int64_t)n_echoes * spe;
     const int tstride = (int)(nmax + 1);
     const int ni = (int)b->images.size();
-    if (b->uploaded && b->tab_words == (size_t)ni * kCand * 2 * tstride &&
+    if (b->uploaded && b->tab_words == (size_t)ni * kCand * tstride &&
         b->acc_words == (size_t)ni * (n_echoes + 1) * kCand * 4)
         return RWNMR_OK;
     b->free_device();
@@ -317,18 +353,17 @@ rwnmr_status upload(rwnmr_batch *b, int n_echoes, int spe)
     BT_CUDA(b, cudaMalloc(&b->d_z, std::max<size_t>(nw, 1) * 4), "batch walkers");
     BT_CUDA(b, cudaMalloc(&b->d_seed, std::max<size_t>(nw, 1) * 8), "batch walkers");
     size_t off = 0;
-    std::vector<int32_t> ushift(ni);
-    const int us = 58 - (int)std::ceil(std::log2((double)(nmax + 2)));
+    // derivative values c f^(c-1) <= nmax: scaled by 2^us so that they stay below 2^57 like the energies
+    const int us = kScaleBits - (int)std::ceil(std::log2((double)(nmax + 2)));
     for (int k = 0; k < ni; k++)
     {
         BT_CUDA(b, cudaMemcpy(b->d_blocks + off, b->h_blocks[k].data(), b->h_blocks[k].size() * 8, cudaMemcpyHostToDevice),
                 "batch image upload");
         b->images[k].blocks = b->d_blocks + off;
         off += b->h_blocks[k].size();
-        b->images[k].tab0 = (int64_t)k * kCand * 2 * tstride;
+        b->images[k].tab0 = (int64_t)k * kCand * tstride;
         b->images[k].acc0 = (int64_t)k * (n_echoes + 1) * kCand * 4;
         b->images[k].u_shift = us;
-        ushift[k] = us;
     }
     if (nw)
     {
@@ -339,9 +374,7 @@ rwnmr_status upload(rwnmr_batch *b, int n_echoes, int spe)
     }
     BT_CUDA(b, cudaMalloc(&b->d_images, std::max(ni, 1) * sizeof(BatchImage)), "batch descriptors");
     BT_CUDA(b, cudaMemcpy(b->d_images, b->images.data(), ni * sizeof(BatchImage), cudaMemcpyHostToDevice), "batch descriptors");
-    BT_CUDA(b, cudaMalloc(&b->d_ushift, std::max(ni, 1) * 4), "batch descriptors");
-    BT_CUDA(b, cudaMemcpy(b->d_ushift, ushift.data(), ni * 4, cudaMemcpyHostToDevice), "batch descriptors");
-    b->tab_words = (size_t)ni * kCand * 2 * tstride;
+    b->tab_words = (size_t)ni * kCand * tstride;
     b->acc_words = (size_t)ni * (n_echoes + 1) * kCand * 4;
     BT_CUDA(b, cudaMalloc(&b->d_tab, std::max<size_t>(b->tab_words, 1) * 8), "batch tables");
     BT_CUDA(b, cudaMalloc(&b->d_acc, std::max<size_t>(b->acc_words, 1) * 8), "batch accumulators");
@@ -379,13 +412,13 @@ rwnmr_status build_items(rwnmr_batch *b, int block)
     return RWNMR_OK;
 }
 
-cudaError_t enqueue(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block)
+cudaError_t enqueue(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block, int wpt)
 {
     const int ni = (int)b->images.size();
     const int tstride = p->n_echoes * p->steps_per_echo + 1;
     cudaError_t e;
     if ((e = cudaMemcpyAsync(b->d_f, b->h_f, (size_t)ni * kCand * 8, cudaMemcpyHostToDevice, b->stream))) return e;
-    batch_tables_kernel<<<(ni * kCand + 127) / 128, 128, 0, b->stream>>>(b->d_f, ni, b->d_ushift, tstride, b->d_tab);
+    batch_tables_kernel<<<(ni * kCand + 127) / 128, 128, 0, b->stream>>>(b->d_f, ni, tstride, b->d_tab);
     if ((e = cudaGetLastError())) return e;
     if ((e = cudaMemsetAsync(b->d_acc, 0, b->acc_words * 8, b->stream))) return e;
     if ((e = cudaMemsetAsync(b->d_counter, 0, 4, b->stream))) return e;
@@ -399,6 +432,7 @@ cudaError_t enqueue(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block)
     L.bc = p->bc;
     L.deriv = p->derivatives ? 1 : 0;
     L.tstride = tstride;
+    L.dshift = ni ? kScaleBits - b->images[0].u_shift : 0;
     L.tab = b->d_tab;
     L.acc = b->d_acc;
     L.x0 = b->d_x;
@@ -414,9 +448,14 @@ cudaError_t enqueue(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block)
         const int grid = std::max(1, std::min(b->n_items, std::max(1, per_sm) * b->sms));
         kern<<<grid, block, smem, b->stream>>>(L);
     };
-    if (p->bc == RWNMR_BC_PERIODIC) occ(batch_cpmg_kernel<BC_PERIODIC>);
-    else if (p->bc == RWNMR_BC_MIRROR) occ(batch_cpmg_kernel<BC_MIRROR>);
-    else occ(batch_cpmg_kernel<BC_NOFLUX>);
+    auto by_wpt = [&](auto bcc) {
+        constexpr int BC = decltype(bcc)::value;
+        if (wpt == 2) occ(batch_cpmg_kernel<BC, 2>);
+        else occ(batch_cpmg_kernel<BC, 1>);
+    };
+    if (p->bc == RWNMR_BC_PERIODIC) by_wpt(std::integral_constant<int, BC_PERIODIC>{});
+    else if (p->bc == RWNMR_BC_MIRROR) by_wpt(std::integral_constant<int, BC_MIRROR>{});
+    else by_wpt(std::integral_constant<int, BC_NOFLUX>{});
     if ((e = cudaGetLastError())) return e;
     if ((e = cudaMemcpyAsync(b->h_acc, b->d_acc, b->acc_words * 8, cudaMemcpyDeviceToHost, b->stream))) return e;
     return cudaMemcpyAsync(b->h_status, b->d_status, 4, cudaMemcpyDeviceToHost, b->stream);
@@ -433,6 +472,8 @@ rwnmr_status check_params(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
     if ((int64_t)p->n_echoes * p->steps_per_echo > (1 << 24)) return put(b->err, RWNMR_ERR_UNSUPPORTED, "walk too long for the batch tables");
     if (p->threads_per_block != 0 && (p->threads_per_block % 32 || p->threads_per_block < 64 || p->threads_per_block > 512))
         return put(b->err, RWNMR_ERR_INVALID, "threads_per_block must be a multiple of 32 in 64..512");
+    if (p->walkers_per_thread < 0 || p->walkers_per_thread > 2)
+        return put(b->err, RWNMR_ERR_INVALID, "walkers_per_thread must be 0 (tuned), 1 or 2");
     return RWNMR_OK;
 }
 } // namespace
@@ -499,10 +540,20 @@ rwnmr_status rwnmr_batch_add_image(rwnmr_batch *b, const uint64_t *blocks, int32
     im.n = n;
     const size_t nb = (size_t)im.bcr * ((nz + 3) / 4);
     b->h_blocks.emplace_back(blocks, blocks + nb);
-    b->hx.insert(b->hx.end(), x0, x0 + n);
-    b->hy.insert(b->hy.end(), y0, y0 + n);
-    b->hz.insert(b->hz.end(), z0, z0 + n);
-    b->hs.insert(b->hs.end(), seed0, seed0 + n);
+    // Walkers are stored in Morton order of their start voxel: a warp then walks neighbouring
+    // walkers, which gather neighbouring bit-blocks and, having similar collision counts, nearby
+    // table entries. Only sums over walkers leave the batch, so the order changes no result.
+    std::vector<std::pair<uint64_t, int64_t>> order((size_t)n);
+    for (int64_t i = 0; i < n; i++) order[(size_t)i] = {morton3(x0[i], y0[i], z0[i]), i};
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<uint64_t, int64_t> &a, const std::pair<uint64_t, int64_t> &c) { return a.first < c.first; });
+    for (const auto &o : order)
+    {
+        b->hx.push_back(x0[o.second]);
+        b->hy.push_back(y0[o.second]);
+        b->hz.push_back(z0[o.second]);
+        b->hs.push_back(seed0[o.second]);
+    }
     b->images.push_back(im);
     b->free_device();
     if (b->d_items) cudaFree(b->d_items);
@@ -527,10 +578,11 @@ rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, 
     cudaSetDevice(b->device);
     if ((st = upload(b, p->n_echoes, p->steps_per_echo)) != RWNMR_OK) return st;
     const int block = p->threads_per_block ? p->threads_per_block : (b->tuned_block ? b->tuned_block : 256);
-    if ((st = build_items(b, block)) != RWNMR_OK) return st;
+    const int wpt = p->walkers_per_thread ? p->walkers_per_thread : (b->tuned_wpt ? b->tuned_wpt : 1);
+    if ((st = build_items(b, block * wpt)) != RWNMR_OK) return st;
     for (int k = 0; k < ni; k++)
         for (int r = 0; r < kCand; r++) b->h_f[k * kCand + r] = r < R ? dfactor[k * R + r] : 1.0;
-    const int key[5] = {p->n_echoes, p->steps_per_echo, p->bc, p->derivatives ? 1 : 0, block};
+    const int key[6] = {p->n_echoes, p->steps_per_echo, p->bc, p->derivatives ? 1 : 0, block, wpt};
     BT_CUDA(b, cudaEventRecord(b->ev0, b->stream), "event");
     if (p->use_graph)
     {
@@ -540,7 +592,7 @@ rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, 
             b->graph = nullptr;
             cudaGraph_t g;
             BT_CUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
-            cudaError_t ce = enqueue(b, p, block);
+            cudaError_t ce = enqueue(b, p, block, wpt);
             cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
             BT_CUDA(b, ce, "graph capture");
             BT_CUDA(b, ee, "graph capture");
@@ -552,7 +604,7 @@ rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, 
         BT_CUDA(b, cudaGraphLaunch(b->graph, b->stream), "graph launch");
     }
     else
-        BT_CUDA(b, enqueue(b, p, block), "batch launch");
+        BT_CUDA(b, enqueue(b, p, block, wpt), "batch launch");
     b->launches += 2;
     BT_CUDA(b, cudaEventRecord(b->ev1, b->stream), "event");
     BT_CUDA(b, cudaStreamSynchronize(b->stream), "batch walk");
@@ -580,7 +632,7 @@ rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, 
 }
 
 rwnmr_status rwnmr_batch_autotune(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int32_t *best_threads,
-                                  double *best_ms)
+                                  int32_t *best_walkers_per_thread, double *best_ms)
 {
     if (!b) return RWNMR_ERR_INVALID;
     rwnmr_status st = check_params(b, p);
@@ -588,22 +640,27 @@ rwnmr_status rwnmr_batch_autotune(rwnmr_batch *b, const rwnmr_batch_cpmg_params 
     const int ni = (int)b->images.size();
     std::vector<double> f((size_t)ni * p->n_candidates, 0.999);
     double best = 1e30;
-    int arg = 256;
-    for (int t : {128, 256, 512})
-    {
-        rwnmr_batch_cpmg_params q = *p;
-        q.threads_per_block = t;
-        q.use_graph = 0;
-        if ((st = rwnmr_batch_cpmg(b, &q, f.data(), nullptr, nullptr)) != RWNMR_OK) return st;
-        if ((st = rwnmr_batch_cpmg(b, &q, f.data(), nullptr, nullptr)) != RWNMR_OK) return st;
-        if (b->last_ms < best)
+    int arg = 256, arg_w = 1;
+    for (int w : {1, 2})
+        for (int t : {128, 256, 512})
         {
-            best = b->last_ms;
-            arg = t;
+            rwnmr_batch_cpmg_params q = *p;
+            q.threads_per_block = t;
+            q.walkers_per_thread = w;
+            q.use_graph = 0;
+            if ((st = rwnmr_batch_cpmg(b, &q, f.data(), nullptr, nullptr)) != RWNMR_OK) return st;
+            if ((st = rwnmr_batch_cpmg(b, &q, f.data(), nullptr, nullptr)) != RWNMR_OK) return st;
+            if (b->last_ms < best)
+            {
+                best = b->last_ms;
+                arg = t;
+                arg_w = w;
+            }
         }
-    }
     b->tuned_block = arg;
+    b->tuned_wpt = arg_w;
     if (best_threads) *best_threads = arg;
+    if (best_walkers_per_thread) *best_walkers_per_thread = arg_w;
     if (best_ms) *best_ms = best;
     return RWNMR_OK;
 }

@@ -301,7 +301,8 @@ class Engine:
 class BatchParams(ctypes.Structure):
     _fields_ = [("bc", ctypes.c_int32), ("steps_per_echo", ctypes.c_int32), ("n_echoes", ctypes.c_int32),
                 ("n_candidates", ctypes.c_int32), ("derivatives", ctypes.c_int32),
-                ("threads_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32)]
+                ("threads_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32),
+                ("walkers_per_thread", ctypes.c_int32)]
 
 
 class Batch:
@@ -344,13 +345,13 @@ class Batch:
         return idx.value
 
     def cpmg(self, dfactor, n_echoes: int, steps_per_echo: int, derivatives: bool = True, bc: str = "noflux",
-             threads_per_block: int = 0, use_graph: bool = True):
+             threads_per_block: int = 0, use_graph: bool = True, walkers_per_thread: int = 0):
         f = np.ascontiguousarray(dfactor, np.float64)
         if f.ndim == 1:
             f = f[:, None]
         R = f.shape[1]
         prm = BatchParams(BC[bc], int(steps_per_echo), int(n_echoes), R, int(bool(derivatives)),
-                          int(threads_per_block), int(bool(use_graph)))
+                          int(threads_per_block), int(bool(use_graph)), int(walkers_per_thread))
         echo = np.zeros((self.n_images, R, n_echoes + 1))
         decho = np.zeros_like(echo) if derivatives else None
         self._check(self.lib.rwnmr_batch_cpmg(self.b, ctypes.byref(prm), _p(f), _p(echo), _p(decho)))
@@ -358,11 +359,13 @@ class Batch:
 
     def autotune(self, n_echoes: int, steps_per_echo: int, n_candidates: int = 16, derivatives: bool = True,
                  bc: str = "noflux"):
-        prm = BatchParams(BC[bc], int(steps_per_echo), int(n_echoes), int(n_candidates), int(bool(derivatives)), 0, 0)
+        prm = BatchParams(BC[bc], int(steps_per_echo), int(n_echoes), int(n_candidates), int(bool(derivatives)), 0, 0, 0)
         t = ctypes.c_int32()
+        wpt = ctypes.c_int32()
         ms = ctypes.c_double()
-        self._check(self.lib.rwnmr_batch_autotune(self.b, ctypes.byref(prm), ctypes.byref(t), ctypes.byref(ms)))
-        return t.value, ms.value
+        self._check(self.lib.rwnmr_batch_autotune(self.b, ctypes.byref(prm), ctypes.byref(t), ctypes.byref(wpt),
+                                                  ctypes.byref(ms)))
+        return t.value, wpt.value, ms.value
 
     @property
     def last_kernel_ms(self) -> float:

@@ -36,6 +36,10 @@ def test_batch_matches_single_image_engine(bc):
     echo, decho = b.cpmg(f, n_echoes, spe, derivatives=True, bc=bc)
     echo2, decho2 = b.cpmg(f, n_echoes, spe, derivatives=True, bc=bc, use_graph=False)
     assert np.array_equal(echo, echo2) and np.array_equal(decho, decho2)
+    # launch shape and walkers per thread do not change the exact sums
+    for t, wpt in ((128, 2), (512, 1), (256, 2)):
+        echo3, decho3 = b.cpmg(f, n_echoes, spe, derivatives=True, bc=bc, threads_per_block=t, walkers_per_thread=wpt)
+        assert np.array_equal(echo3, echo) and np.array_equal(decho3, decho)
     eng = Engine(0)
     for k, (lab, blocks, w) in enumerate(imgs):
         eng.upload_labels(lab, 1)
@@ -55,8 +59,8 @@ def test_batch_autotune_and_fewer_candidates():
     b = Batch(0)
     for lab, blocks, w in imgs:
         b.add_image(blocks, lab.shape, *w)
-    t, ms = b.autotune(20, 2, 16)
-    assert t in (128, 256, 512) and ms > 0
+    t, wpt, ms = b.autotune(20, 2, 16)
+    assert t in (128, 256, 512) and wpt in (1, 2) and ms > 0
     f = dfactor(np.array([[10.0, 20.0], [5.0, 30.0], [40.0, 2.0]]))
     echo, _ = b.cpmg(f, 20, 2, derivatives=False)
     assert echo.shape == (3, 2, 21)
