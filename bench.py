@@ -274,7 +274,7 @@ def run_fit_batch(args):
 
     small = args.workload.endswith("-small")
     n_img = 8 if small else 64
-    echoes, spe, t2b = (300 if small else 3000), 3, 2800.0
+    echoes, spe, t2b = args.echoes or (300 if small else 3000), 3, 2800.0
     rng = np.random.default_rng(100)
     specs = []
     for k in range(n_img):
@@ -327,7 +327,7 @@ def run_fit_batch(args):
             "config": {"workload": args.workload, "images": n_img, "walkers_total": int(nwalk.sum()),
                        "echoes": echoes, "steps_per_echo": spe, "candidates": 16,
                        "walker_steps_per_pass": steps_per_pass, "autotuned_threads": tuned, "autotuned_walkers_per_thread": tuned_wpt,
-                       "autotune_walk_ms": tune_ms,
+                       "autotune_best_walk_ms": tune_ms,
                        "setup_seconds": setup_s},
             "batched_fit": {"gpu_seconds": fit["gpu_seconds"], "passes": fit["walks"],
                             "walker_steps_per_s_per_pass": steps_per_pass * fit["walks"] / fit["gpu_seconds"],
@@ -501,6 +501,7 @@ def main():
     ap.add_argument("--ga-generations", type=int, default=50)
     ap.add_argument("--fit-evals", type=int, default=40)
     ap.add_argument("--fit-iters", type=int, default=6)
+    ap.add_argument("--echoes", type=int, default=0, help="rho-fit-batch: echo count override (profiling)")
     args = ap.parse_args()
     if args.workload.startswith("rho-fit-multiphase"):
         return run_fit_multiphase(args)
