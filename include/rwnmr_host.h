@@ -62,6 +62,45 @@ int rwnmr_cli_main(int argc, const char *const *argv);
 int64_t rwnmr_png_solid_mask(const char *path, int32_t *width, int32_t *height, uint8_t *mask, char *err,
                              int32_t errlen);
 
+/* T2 distribution of a CPMG decay (Tikhonov-regularised non-negative inverse Laplace transform),
+ * replacing the reference's NMRInverter as NMR_cpmg::applyLaplace runs it
+ * (NMR_Simulation/NMR_cpmg.cpp:387-453; Laplace/src/nmrinv_core.cpp, TikhonovSolver.cpp,
+ * Laplace/include/NNLS.hpp). Fields are the cpmg config keys of the same names. */
+typedef struct rwnmr_t2_config
+{
+    double min_t2, max_t2;         /* MIN_T2, MAX_T2 (ms) */
+    int32_t use_logspace;          /* USE_T2_LOGSPACE */
+    int32_t num_t2_bins;           /* NUM_T2_BINS */
+    double min_lambda, max_lambda; /* MIN_LAMBDA, MAX_LAMBDA (log10 of the Tikhonov parameter) */
+    int32_t num_lambdas;           /* NUM_LAMBDAS */
+    int32_t prune_num;             /* PRUNE_NUM (0: no prune-averaging) */
+    double noise_amp;              /* NOISE_AMP: std of Gaussian noise added before inverting (0: none) */
+    uint64_t noise_seed;           /* seed of that noise (the reference draws it from std::random_device) */
+} rwnmr_t2_config;
+
+/* Inverts the decay (times[i], amps[i]), i < n, whose first point is t = 0 (dropped, as the
+ * reference does): noise, prune-averaging to prune_num points, the L-curve choice of lambda, NNLS on
+ * [K; lambda I]. Writes num_t2_bins bins and amplitudes, the chosen lambda and (nullable) the noise
+ * added to each of the n points (noise[0] = 0). Returns num_t2_bins, or -1 with the message in err. */
+int32_t rwnmr_t2_invert(const double *times, const double *amps, int32_t n, const rwnmr_t2_config *cfg,
+                        double *t2_bins, double *t2_amps, double *lambda, double *noise, char *err, int32_t errlen);
+
+/* The steps of rwnmr_t2_invert, exported for tests and for callers that build their own kernels.
+ * Prune-averaging (nmrinv_core.cpp:145-239): returns prune_num and writes prune_num points, or 0 if
+ * the decay is not longer than prune_num (no pruning), -1 on bad arguments. */
+int32_t rwnmr_t2_prune(const double *times, const double *amps, int32_t n, int32_t prune_num, double *out_times,
+                       double *out_amps);
+/* L-curve over 10^linspace(min_lambda, max_lambda, num_lambdas) for the column-major m x n kernel a
+ * and data b (TikhonovSolver.cpp:14-116): writes the curvature per lambda and the non-zero singular
+ * values (count in *n_singular); returns the index of the first curvature maximum, -1 on error. */
+int32_t rwnmr_t2_lcurve(const double *a, int32_t m, int32_t n, const double *b, double min_lambda,
+                        double max_lambda, int32_t num_lambdas, double *curvature, double *singular_values,
+                        int32_t *n_singular);
+/* Non-negative least squares min ||a x - b||, x >= 0, a column-major m x n (Lawson-Hanson, the
+ * algorithm of Laplace/include/NNLS.hpp:289-406). max_solves <= 0: 50 (n + 1). Returns the number of
+ * least-squares solves, or -1 (bad arguments or no convergence). */
+int32_t rwnmr_nnls(const double *a, int32_t m, int32_t n, const double *b, double *x, int32_t max_solves);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,9 +12,11 @@
 #include <iomanip>
 #include <iostream>
 #include <limits>
+#include <random>
 #include <sstream>
 
 #include "host_internal.h"
+#include "laplace.h"
 #include "rwnmr_host.h"
 
 namespace rwnmr_host
@@ -543,9 +545,51 @@ bool CpmgSequence::run_simulation(std::string &err)
         const double norm = 1.0 / amps[0];
         for (double &a : amps) a = norm * a;
     }
-    // applyLaplace needs the reference's Eigen-based inverter, which stays outside this build:
-    // the decay's noise column is zero and cpmg_T2.csv holds only its header.
     noise.assign(amps.size(), 0.0);
+    t2_bins.clear();
+    t2_amps.clear();
+    return true;
+}
+
+bool CpmgSequence::apply_laplace(std::string &err)
+{
+    // Tikhonov-ILT of the normalised decay without its t = 0 point; with NOISE_AMP the inverted
+    // decay carries Gaussian noise, which becomes the decay file's noise column.
+    t2_bins.clear();
+    t2_amps.clear();
+    if (amps.size() < 3 || times.size() != amps.size())
+    {
+        sim.log("- T2 inversion skipped: the decay has fewer than 3 points");
+        return true;
+    }
+    T2InversionConfig c;
+    c.min_t2 = cfg.min_t2;
+    c.max_t2 = cfg.max_t2;
+    c.use_logspace = cfg.use_t2_logspace;
+    c.num_t2_bins = cfg.num_t2_bins;
+    c.min_lambda = cfg.min_lambda;
+    c.max_lambda = cfg.max_lambda;
+    c.num_lambdas = cfg.num_lambdas;
+    c.prune_num = cfg.prune_num;
+    c.noise_amp = cfg.noise_amp;
+    c.noise_seed = sim.rw.seed;
+    if (c.noise_amp != 0.0 && c.noise_seed == 0)
+    {
+        std::random_device dev;
+        c.noise_seed = ((uint64_t)dev() << 32) | dev();
+    }
+    T2Inversion r;
+    if (!invert_t2(times, amps, c, r, err)) return false;
+    t2_bins = r.bins;
+    t2_amps = r.amps;
+    t2_lambda = r.lambda;
+    noise.assign(amps.size(), 0.0);
+    if (r.noise.size() + 1 == amps.size())
+        for (size_t i = 1; i < amps.size(); i++) noise[i] = r.noise[i - 1];
+    std::ostringstream m;
+    m << "- T2 inversion: " << t2_bins.size() << " bins, filtering lambda " << t2_lambda << ", "
+      << r.nnls_solves << " NNLS solves";
+    sim.log(m.str());
     return true;
 }
 
@@ -558,8 +602,10 @@ void CpmgSequence::save() const
         f << "time,signal,noise,noiseless\n";
         for (size_t i = 0; i < amps.size(); i++)
             f << times[i] << "," << amps[i] + noise[i] << "," << noise[i] << "," << amps[i] << "\n";
+        // writeT2dist (NMR_cpmg.cpp:514-535)
         std::ofstream t = open_out(dir + "/cpmg_T2.csv");
         t << "NMRT2_bins,NMRT2_amps\n";
+        for (size_t i = 0; i < t2_bins.size() && i < t2_amps.size(); i++) t << t2_bins[i] << "," << t2_amps[i] << "\n";
         if (!echo_collisions.empty())
         {
             // per-echo collision counts per phase (an output the reference does not have)
@@ -612,7 +658,7 @@ void CpmgSequence::save() const
 
 bool CpmgSequence::run(std::string &err)
 {
-    if (!set(err) || !run_simulation(err)) return false;
+    if (!set(err) || !run_simulation(err) || !apply_laplace(err)) return false;
     save();
     sim.log("- CPMG: " + std::to_string(sim.echoes) + " echoes x " + std::to_string(sim.rw.steps_per_echo) +
             " steps, walk " + std::to_string(kernel_ms) + " ms on the GPU");
@@ -717,6 +763,8 @@ bool MultitauSequence::run(std::string &err)
         if (seq.amps.size() > 1) signal_amps.push_back(seq.amps[1]);
         if (cfg.complete_decay)
         {
+            // runCPMG inverts complete decays (NMR_multitau.cpp:146-149)
+            if (!seq.apply_laplace(err)) return false;
             // saveCPMG (NMR_multitau.cpp:154-185): the multitau SAVE_* flags pick the files
             seq.cfg.save_mode = true;
             seq.cfg.save_walkers = cfg.save_walkers;

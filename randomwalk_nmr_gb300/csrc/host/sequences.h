@@ -97,12 +97,15 @@ class CpmgSequence
     bool map = true;            // NMR_cpmg::setNMRTimeFramework(_map)
     std::string name, dir;
     std::vector<double> times, amps, raw, noise;
+    std::vector<double> t2_bins, t2_amps;  // T2 distribution (apply_laplace)
+    double t2_lambda = 0.0;
     std::vector<uint64_t> echo_collisions; // [echoes][phases]
     double kernel_ms = 0.0;
     CpmgSequence(Simulation &s, const CpmgConfig &c) : sim(s), cfg(c) {}
     bool run(std::string &err); // set + run_simulation + save (NMR_cpmg::run, NMR_cpmg.cpp:87-93)
     bool set(std::string &err);
     bool run_simulation(std::string &err);
+    bool apply_laplace(std::string &err); // NMR_cpmg::applyLaplace (NMR_cpmg.cpp:387-453)
     void save() const;
 };
 

@@ -11,7 +11,16 @@ from .engine import load_library
 _vp = ctypes.c_void_p
 
 HOST_EXPORTS = ["rwnmr_synth_spheres", "rwnmr_pack_blocks", "rwnmr_place_walkers", "rwnmr_png_solid_mask",
-                "rwnmr_config_json", "rwnmr_cli_main"]
+                "rwnmr_config_json", "rwnmr_cli_main", "rwnmr_t2_invert", "rwnmr_t2_prune", "rwnmr_t2_lcurve",
+                "rwnmr_nnls"]
+
+
+class T2Config(ctypes.Structure):
+    """rwnmr_t2_config: the cpmg config's Laplace-inversion keys."""
+    _fields_ = [("min_t2", ctypes.c_double), ("max_t2", ctypes.c_double), ("use_logspace", ctypes.c_int32),
+                ("num_t2_bins", ctypes.c_int32), ("min_lambda", ctypes.c_double), ("max_lambda", ctypes.c_double),
+                ("num_lambdas", ctypes.c_int32), ("prune_num", ctypes.c_int32), ("noise_amp", ctypes.c_double),
+                ("noise_seed", ctypes.c_uint64)]
 
 
 class PlacementInfo(ctypes.Structure):
@@ -25,6 +34,8 @@ def _lib():
     L.rwnmr_pack_blocks.restype = ctypes.c_int64
     L.rwnmr_place_walkers.restype = ctypes.c_int
     L.rwnmr_png_solid_mask.restype = ctypes.c_int64
+    for name in ("rwnmr_t2_invert", "rwnmr_t2_prune", "rwnmr_t2_lcurve", "rwnmr_nnls"):
+        getattr(L, name).restype = ctypes.c_int32
     return L
 
 
@@ -100,3 +111,64 @@ def cli(args, cwd=None) -> int:
         return int(L.rwnmr_cli_main(len(argv), arr))
     finally:
         os.chdir(old)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def invert_t2(times, amps, min_t2=0.1, max_t2=10000.0, use_logspace=True, num_t2_bins=128, min_lambda=-4.0,
+              max_lambda=2.0, num_lambdas=512, prune_num=512, noise_amp=0.0, noise_seed=0):
+    """T2 distribution of a decay whose first point is t = 0 (rwnmr_t2_invert; the defaults are the
+    reference's cpmg.config). Returns (bins, amps, lambda, noise per decay point)."""
+    t, a = _f64(times), _f64(amps)
+    if t.shape != a.shape or t.ndim != 1:
+        raise ValueError("times and amps must be 1-D of equal length")
+    cfg = T2Config(min_t2, max_t2, int(bool(use_logspace)), num_t2_bins, min_lambda, max_lambda, num_lambdas,
+                   prune_num, noise_amp, noise_seed)
+    bins = np.zeros(max(num_t2_bins, 0))
+    out = np.zeros_like(bins)
+    noise = np.zeros_like(t)
+    lam = ctypes.c_double(0.0)
+    err = ctypes.create_string_buffer(512)
+    n = _lib().rwnmr_t2_invert(_p(t), _p(a), len(t), ctypes.byref(cfg), _p(bins), _p(out), ctypes.byref(lam),
+                               _p(noise), err, 512)
+    if n < 0:
+        raise ValueError(err.value.decode())
+    return bins, out, lam.value, noise
+
+
+def prune_decay(times, amps, prune_num: int):
+    """Prune-averaged (times, amps) of a decay (without its t = 0 point), or None when the decay is
+    not longer than prune_num."""
+    t, a = _f64(times), _f64(amps)
+    ot, oa = np.zeros(max(prune_num, 0)), np.zeros(max(prune_num, 0))
+    n = _lib().rwnmr_t2_prune(_p(t), _p(a), len(t), prune_num, _p(ot), _p(oa))
+    if n < 0:
+        raise ValueError("bad arguments")
+    return None if n == 0 else (ot, oa)
+
+
+def lcurve(A, b, min_lambda=-4.0, max_lambda=2.0, num_lambdas=512):
+    """(best index, curvature per lambda, singular values) of the Tikhonov L-curve for kernel A."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    m, n = A.shape
+    curv = np.zeros(num_lambdas)
+    sv = np.zeros(min(m, n))
+    ns = ctypes.c_int32(0)
+    best = _lib().rwnmr_t2_lcurve(A.ctypes.data_as(_vp), m, n, _p(_f64(b)), ctypes.c_double(min_lambda),
+                                  ctypes.c_double(max_lambda), num_lambdas, _p(curv), _p(sv), ctypes.byref(ns))
+    if best < 0:
+        raise ValueError("bad arguments")
+    return best, curv, sv[:ns.value]
+
+
+def nnls(A, b, max_solves: int = 0):
+    """x >= 0 minimising ||A x - b|| (rwnmr_nnls). Returns (x, least-squares solves)."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    m, n = A.shape
+    x = np.zeros(n)
+    r = _lib().rwnmr_nnls(A.ctypes.data_as(_vp), m, n, _p(_f64(b)), _p(x), max_solves)
+    if r < 0:
+        raise ValueError("NNLS failed (bad arguments or no convergence)")
+    return x, r

@@ -42,6 +42,23 @@ def test_cli_cpmg_matches_reference_sequence(tmp_path, golden):
     walkers = np.loadtxt(d + "/cpmg_walkers.csv", delimiter=",", skiprows=1)
     assert np.array_equal(walkers[:, 6].astype(np.int64), golden["cpmg_map_collisions"].astype(np.int64))
     assert os.path.exists(str(tmp_path / "db" / "t" / "SimInfo.txt"))
+    check_t2_file(d, decay)
+
+
+def check_t2_file(d, decay, bins=128):
+    """cpmg_T2.csv is the T2 inversion of the decay beside it (default cpmg.config settings): the
+    oracle's restatement at the oracle's L-curve choice or at a grid neighbour (the curvature's
+    flat maximum moves a step between SVD implementations on noisy decays)."""
+    from oracle import laplace
+
+    t2 = np.loadtxt(d + "/cpmg_T2.csv", delimiter=",", skiprows=1)
+    assert t2.shape == (bins, 2) and np.all(t2[:, 1] >= 0)
+    r = laplace.invert(decay[:, 0], decay[:, 3], num_t2_bins=bins)
+    assert np.array_equal(t2[:, 0], r["bins"])
+    near = range(max(0, r["best"] - 2), min(len(r["lambdas"]), r["best"] + 3))
+    cands = [laplace.invert(decay[:, 0], decay[:, 3], num_t2_bins=bins, force_lambda=r["lambdas"][k])["amps"]
+             for k in near]
+    assert min(np.max(np.abs(t2[:, 1] - c)) / np.max(c) for c in cands) <= 1e-8
 
 
 def test_cli_cpmg_internal_field(tmp_path, golden, oracle):
@@ -126,6 +143,7 @@ def test_cli_multitau_matches_reference(tmp_path, golden, complete):
     if complete:
         decay = np.loadtxt(te0 + "/cpmg_decay.csv", delimiter=",", skiprows=1)
         assert len(decay) == 91 and decay[1, 1] == mt[0, 1]  # 12 ms / (2 steps x 1/15 ms) echoes + t = 0
+        check_t2_file(te0, decay)
     else:
         assert os.path.isdir(te0) and not os.path.exists(te0 + "/cpmg_decay.csv")
 
