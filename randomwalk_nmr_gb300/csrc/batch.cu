@@ -150,7 +150,9 @@ __global__ void __launch_bounds__(512, 2) batch_cpmg_kernel(BatchLaunch L)
                 init_image_coords<BC>(im, p[j]);
             }
         }
-        const unsigned long long *tabE = L.tab + img.tab0;
+        // candidate pairs interleaved: entry (r, c) at ((r / 2) * tstride + c) * 2 + r % 2, so one
+        // 16-byte load returns two candidates' values for a walker
+        const ulonglong2 *tab2 = reinterpret_cast<const ulonglong2 *>(L.tab + img.tab0);
         unsigned long long *acc = L.acc + img.acc0;
         for (int k = threadIdx.x; k < kWin * kCand * 4; k += blockDim.x) sacc[k] = 0;
         __syncthreads();
@@ -172,13 +174,17 @@ __global__ void __launch_bounds__(512, 2) batch_cpmg_kernel(BatchLaunch L)
                         }
                 unsigned long long v[kCand];
 #pragma unroll
-                for (int r = 0; r < kCand; r++)
-                {
-                    v[r] = 0;
+                for (int r = 0; r < kCand; r++) v[r] = 0;
+#pragma unroll
+                for (int q = 0; q < kCand / 2; q++)
 #pragma unroll
                     for (int j = 0; j < WPT; j++)
-                        v[r] += active[j] ? __ldg(tabE + (size_t)r * L.tstride + c[j]) : 0ull;
-                }
+                        if (active[j])
+                        {
+                            const ulonglong2 t = __ldg(tab2 + (size_t)q * L.tstride + c[j]);
+                            v[2 * q] += t.x;
+                            v[2 * q + 1] += t.y;
+                        }
                 const unsigned long long sumE = transpose_reduce16(v, lane);
                 const int slot = e - (e0 + 1);
                 // a warp sum is below 2^63; its 32-bit halves accumulate without overflow
@@ -191,13 +197,17 @@ __global__ void __launch_bounds__(512, 2) batch_cpmg_kernel(BatchLaunch L)
                 if (L.deriv)
                 {
 #pragma unroll
-                    for (int r = 0; r < kCand; r++)
-                    {
-                        v[r] = 0;
+                    for (int r = 0; r < kCand; r++) v[r] = 0;
+#pragma unroll
+                    for (int q = 0; q < kCand / 2; q++)
 #pragma unroll
                         for (int j = 0; j < WPT; j++)
-                            v[r] += (active[j] && c[j]) ? (unsigned long long)c[j] * (__ldg(tabE + (size_t)r * L.tstride + c[j] - 1) >> L.dshift) : 0ull;
-                    }
+                            if (active[j] && c[j])
+                            {
+                                const ulonglong2 t = __ldg(tab2 + (size_t)q * L.tstride + c[j] - 1);
+                                v[2 * q] += (unsigned long long)c[j] * (t.x >> L.dshift);
+                                v[2 * q + 1] += (unsigned long long)c[j] * (t.y >> L.dshift);
+                            }
                     const unsigned long long sumU = transpose_reduce16(v, lane);
                     if ((lane & 1) == 0)
                     {
@@ -228,11 +238,12 @@ __global__ void batch_tables_kernel(const double *__restrict__ f, int n_images, 
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_images * kCand) return;
     const double fr = f[t];
-    unsigned long long *te = tab + (size_t)t * tstride;
+    const int img = t / kCand, r = t % kCand;
+    unsigned long long *te = tab + ((size_t)img * kCand + (r & ~1)) * tstride + (r & 1);
     double v = 1.0;
     for (int k = 0; k < tstride; k++)
     {
-        te[k] = __double2ull_rn(v * kEScale);
+        te[2 * k] = __double2ull_rn(v * kEScale);
         v = v * fr;
     }
 }
