@@ -263,8 +263,10 @@ def run_fit_multiphase(args):
 
 def run_fit_batch(args):
     """Batched uneven workload: 64 sphere packs with edges U[64, 320], walkers
-    U[1e4, 5e5], 16 relaxivity candidates per image, 3000 echoes of 3 steps, one persistent launch per
-    fit iteration (CUDA graph, autotuned block size), vs per-image plain CPMG + the restated GA."""
+    U[1e4, 5e5], 16 relaxivity candidates per image, 3000 echoes of 3 steps: one persistent histogram
+    walk (autotuned block shape) keeps every image's per-echo collision histograms, then each fit
+    iteration evaluates all candidates and derivatives from them (CUDA graph); vs per-image plain
+    CPMG + the restated GA."""
     from concurrent.futures import ThreadPoolExecutor
 
     from randomwalk_nmr_gb300 import Batch, Engine
@@ -274,6 +276,7 @@ def run_fit_batch(args):
 
     small = args.workload.endswith("-small")
     n_img = 8 if small else 64
+    n_use = min(args.images or n_img, n_img)
     echoes, spe, t2b = args.echoes or (300 if small else 3000), 3, 2800.0
     rng = np.random.default_rng(100)
     specs = []
@@ -282,6 +285,8 @@ def run_fit_batch(args):
         nw = int(rng.integers(10_000, 500_001)) if not small else int(rng.integers(2_000, 20_001))
         specs.append(((edge,) * 3, 3.0, 15.0, float(rng.uniform(0.15, 0.40)), 1, 100 + k, nw, 1000 + k))
     t0 = time.perf_counter()
+    specs = specs[:n_use]
+    n_img = n_use
     with ThreadPoolExecutor(os.cpu_count() or 4) as ex:
         imgs = list(ex.map(_sphere_image, specs))
     setup_s = time.perf_counter() - t0
@@ -295,11 +300,14 @@ def run_fit_batch(args):
     hidden = rng.uniform(2.0, 50.0, n_img)
     fh = np.ones((n_img, 16))
     fh[:, 0] = decrease_factor(hidden)
-    echo, _ = b.cpmg(fh, echoes, spe, derivatives=False)
+    # targets by the candidate walk, which stores no histograms: the fit's first call does (and is
+    # charged for) the histogram walk
+    echo, _ = b.cpmg(fh, echoes, spe, derivatives=False, method="walk")
     bulk = np.exp(-echo_times(echoes, spe, 1.0 / 15.0) / t2b)
     targets = echo[:, 0] / nwalk[:, None] * bulk + rng.normal(0.0, 1e-3, (n_img, echoes + 1))
     rho0 = rng.uniform(2.0, 50.0, (n_img, 16))
     fit = fit_rho_batch(b, targets, nwalk, echoes, spe, t2b, rho0, iters=args.fit_iters)
+    hist_walk_s = b.histogram_walk_ms * 1e-3
     steps_per_pass = int(nwalk.sum()) * echoes * spe
     # plain per-image CPMG: one walk per image per GA evaluation
     eng = Engine(0)
@@ -329,8 +337,10 @@ def run_fit_batch(args):
                        "walker_steps_per_pass": steps_per_pass, "autotuned_threads": tuned, "autotuned_walkers_per_thread": tuned_wpt,
                        "autotune_best_walk_ms": tune_ms,
                        "setup_seconds": setup_s},
-            "batched_fit": {"gpu_seconds": fit["gpu_seconds"], "passes": fit["walks"],
-                            "walker_steps_per_s_per_pass": steps_per_pass * fit["walks"] / fit["gpu_seconds"],
+            "batched_fit": {"gpu_seconds": fit["gpu_seconds"], "passes": fit["walks"], "method": "histograms",
+                            "histogram_walk_seconds": hist_walk_s,
+                            "histogram_walk_walker_steps_per_s": steps_per_pass / max(hist_walk_s, 1e-12),
+                            "evaluation_ms_per_pass": (fit["gpu_seconds"] - hist_walk_s) * 1e3 / fit["walks"],
                             "max_abs_rho_error": float(np.max(np.abs(fit["rho"] - hidden))),
                             "median_abs_rho_error": float(np.median(np.abs(fit["rho"] - hidden)))},
             "per_image_cpmg_ga": {"gpu_seconds_estimate": ga_gpu, "plain_walk_gpu_seconds_all_images":
@@ -502,6 +512,7 @@ def main():
     ap.add_argument("--fit-evals", type=int, default=40)
     ap.add_argument("--fit-iters", type=int, default=6)
     ap.add_argument("--echoes", type=int, default=0, help="rho-fit-batch: echo count override (profiling)")
+    ap.add_argument("--images", type=int, default=0, help="rho-fit-batch: use the first N images (profiling)")
     args = ap.parse_args()
     if args.workload.startswith("rho-fit-multiphase"):
         return run_fit_multiphase(args)

@@ -204,8 +204,21 @@ rwnmr_status rwnmr_cpmg_run_noalloc(const rwnmr_cpmg_params *p, const rwnmr_noal
  * the relaxivity). Per image and candidate the walk returns the normalisation-free echo sums
  * M_r(e) = sum_w f_r^c_w(e) and, if asked, their exact derivatives dM_r(e)/df_r =
  * sum_w c_w f_r^(c_w - 1), from which any loss gradient (the adjoint for that candidate) follows on
- * the host. Single-phase images (labels != 0 are solid). */
+ * the host. Single-phase images (labels != 0 are solid).
+ * Two methods give identical sums. RWNMR_BATCH_HISTOGRAMS walks every walker once per (n_echoes,
+ * steps_per_echo, bc) and keeps exact integer per-echo collision-count histograms H[image][e][c]
+ * (walkers with c collisions after echo e) on the device; every call then evaluates
+ * M_r(e) = sum_c H[e][c] f_r^c and its derivative from them without walking (the reference's
+ * `histogram` CPMG method, NMR_cpmg.cpp:235-343, bins collision rates approximately instead).
+ * RWNMR_BATCH_CANDIDATE_WALK walks on every call and adds up the candidates walker by walker. */
 typedef struct rwnmr_batch rwnmr_batch;
+
+enum
+{
+    RWNMR_BATCH_AUTO = 0,           /* histograms if they fit in half the free device memory */
+    RWNMR_BATCH_HISTOGRAMS = 1,
+    RWNMR_BATCH_CANDIDATE_WALK = 2
+};
 
 typedef struct rwnmr_batch_cpmg_params
 {
@@ -218,6 +231,8 @@ typedef struct rwnmr_batch_cpmg_params
     int32_t use_graph;         /* replay the launch sequence as a captured CUDA graph */
     int32_t walkers_per_thread; /* 1 or 2; 0 = autotuned value (or 1 before rwnmr_batch_autotune).
                                    Results do not depend on it (exact integer sums). */
+    int32_t method;             /* RWNMR_BATCH_*; histograms take 4 * (n_echoes + 1 + steps_per_echo *
+                                   n_echoes * (n_echoes + 1) / 2) bytes per image */
 } rwnmr_batch_cpmg_params;
 
 rwnmr_status rwnmr_batch_create(rwnmr_batch **out, int device);
@@ -232,10 +247,19 @@ rwnmr_status rwnmr_batch_add_image(rwnmr_batch *batch, const uint64_t *blocks, i
 /* dfactor [n_images][n_candidates]; echo and decho (nullable) [n_images][n_candidates][n_echoes+1]. */
 rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *batch, const rwnmr_batch_cpmg_params *p, const double *dfactor,
                               double *echo, double *decho);
-/* Times the walk for 128, 256 and 512 threads per block with 1 and 2 walkers per thread and keeps
- * the fastest pair for later calls (outputs nullable). */
+/* Times the walk of the method p selects (the histogram walk, or the candidate walk) for 128, 256
+ * and 512 threads per block with 1 and 2 walkers per thread and keeps the fastest pair for later
+ * calls (outputs nullable). */
 rwnmr_status rwnmr_batch_autotune(rwnmr_batch *batch, const rwnmr_batch_cpmg_params *p, int32_t *best_threads,
                                   int32_t *best_walkers_per_thread, double *best_ms);
+/* Row `echo` of image `image`'s collision histogram from the last histogram walk: counts[c] =
+ * walkers with c collisions after that echo, c = 0 .. steps_per_echo * echo (*n_counts entries;
+ * counts NULL: size only). */
+rwnmr_status rwnmr_batch_collision_histogram(rwnmr_batch *batch, int32_t image, int32_t echo, uint32_t *counts,
+                                             int32_t *n_counts);
+/* GPU time of the last histogram walk (ms); rwnmr_batch_last_kernel_ms includes it in the call
+ * that ran it. */
+double rwnmr_batch_histogram_walk_ms(const rwnmr_batch *batch);
 
 /* ---- collision-mapping walk ------------------------------------------------------------ */
 /* NMR_Simulation::mapSimulation (NMR_Simulation.cpp:1787-1841; NMR_Simulation_cuda.cpp:726-1270):

@@ -49,6 +49,7 @@ struct BatchImage
     int64_t walker0, n;       // walker range in the batch arrays
     int64_t acc0;             // offset of this image's accumulators (u64 words)
     int64_t tab0;             // offset of this image's tables (u64 words)
+    int64_t hist0;            // offset of this image's collision histogram (u32 words)
     int32_t u_shift;          // derivative scale exponent
 };
 
@@ -74,7 +75,58 @@ struct BatchLaunch
     const uint64_t *seed0;
     unsigned *counter;
     unsigned *status;
+    unsigned *hist;                // collision histograms (histogram walk), see hist_row
 };
+
+// Per-echo collision histograms: after echo e a walker has at most steps_per_echo * e collisions,
+// so row e of an image's histogram holds the walker counts for c = 0 .. spe * e and starts at
+// hist_row(e) = sum over earlier rows of their lengths (a triangular layout: half a dense table).
+__host__ __device__ __forceinline__ int64_t hist_row(int64_t e, int spe) { return e + (int64_t)spe * e * (e - 1) / 2; }
+__host__ __device__ __forceinline__ int64_t hist_words(int64_t n_echoes, int spe) { return hist_row(n_echoes + 1, spe); }
+
+__device__ __forceinline__ DevImage dev_image(const BatchImage &img, int bc)
+{
+    DevImage im;
+    im.blocks = img.blocks;
+    im.nx = img.nx;
+    im.ny = img.ny;
+    im.nz = img.nz;
+    im.bcols = img.bcols;
+    im.bcr = img.bcr;
+    im.bc = bc;
+    im.shift = 0;
+    return im;
+}
+
+// Loads the walkers of work item w that this thread walks: first + threadIdx.x + j * blockDim.x.
+template <int BC, int WPT>
+__device__ __forceinline__ void load_walkers(const BatchLaunch &L, const WorkItem &w, const DevImage &im,
+                                             WalkerPos (&p)[WPT], uint64_t (&seed)[WPT], bool (&active)[WPT],
+                                             uint32_t (&c)[WPT])
+{
+#pragma unroll
+    for (int j = 0; j < WPT; j++)
+    {
+        p[j] = WalkerPos{};
+        seed[j] = 0;
+        c[j] = 0;
+        const int64_t i = w.first + threadIdx.x + (int64_t)j * blockDim.x;
+        active[j] = i < w.last;
+        if (active[j])
+        {
+            p[j].x = L.x0[i];
+            p[j].y = L.y0[i];
+            p[j].z = L.z0[i];
+            seed[j] = L.seed0[i];
+            if (!start_ok<BC>(im, p[j]))
+            {
+                atomicOr(L.status, kStatusBadStart);
+                active[j] = false;
+            }
+            init_image_coords<BC>(im, p[j]);
+        }
+    }
+}
 
 // Sum over the warp of v[0..15] per candidate: after the exchanges lane l holds candidate l >> 1's
 // warp total (lanes 2c and 2c+1 hold the same value).
@@ -115,41 +167,12 @@ __global__ void __launch_bounds__(512, 2) batch_cpmg_kernel(BatchLaunch L)
         if (item >= L.n_items) break;
         const WorkItem w = L.items[item];
         const BatchImage img = L.images[w.image];
-        DevImage im;
-        im.blocks = img.blocks;
-        im.nx = img.nx;
-        im.ny = img.ny;
-        im.nz = img.nz;
-        im.bcols = img.bcols;
-        im.bcr = img.bcr;
-        im.bc = L.bc;
-        im.shift = 0;
+        const DevImage im = dev_image(img, L.bc);
         WalkerPos p[WPT];
         uint64_t seed[WPT];
         bool active[WPT];
         uint32_t c[WPT];
-#pragma unroll
-        for (int j = 0; j < WPT; j++)
-        {
-            p[j] = WalkerPos{};
-            seed[j] = 0;
-            c[j] = 0;
-            const int64_t i = w.first + threadIdx.x + (int64_t)j * blockDim.x;
-            active[j] = i < w.last;
-            if (active[j])
-            {
-                p[j].x = L.x0[i];
-                p[j].y = L.y0[i];
-                p[j].z = L.z0[i];
-                seed[j] = L.seed0[i];
-                if (!start_ok<BC>(im, p[j]))
-                {
-                    atomicOr(L.status, kStatusBadStart);
-                    active[j] = false;
-                }
-                init_image_coords<BC>(im, p[j]);
-            }
-        }
+        load_walkers<BC, WPT>(L, w, im, p, seed, active, c);
         // candidate pairs interleaved: entry (r, c) at ((r / 2) * tstride + c) * 2 + r % 2, so one
         // 16-byte load returns two candidates' values for a walker
         const ulonglong2 *tab2 = reinterpret_cast<const ulonglong2 *>(L.tab + img.tab0);
@@ -229,6 +252,134 @@ __global__ void __launch_bounds__(512, 2) batch_cpmg_kernel(BatchLaunch L)
     }
 }
 
+// Histogram walk: every walker of every image walks once and, after each echo e (and at e = 0),
+// adds one to H[image][e][c] for its collision count c. Trajectories do not depend on the
+// relaxivity, so these counts give every candidate's echo sums exactly:
+//   sum_w f^c_w(e) = sum_c H[e][c] f^c   (batch_eval_kernel).
+// The increments are fire-and-forget atomics; the rows a CTA is filling (its walkers share the
+// echo) stay in L2.
+template <int BC, int WPT>
+__global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
+{
+    __shared__ int s_item;
+    for (;;)
+    {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(L.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= L.n_items) break;
+        const WorkItem w = L.items[item];
+        const BatchImage img = L.images[w.image];
+        const DevImage im = dev_image(img, L.bc);
+        WalkerPos p[WPT];
+        uint64_t seed[WPT];
+        bool active[WPT];
+        uint32_t c[WPT];
+        load_walkers<BC, WPT>(L, w, im, p, seed, active, c);
+        unsigned *H = L.hist + img.hist0;
+        const int spe = L.steps_per_echo;
+        for (int e = 0; e <= L.n_echoes; e++)
+        {
+            const int64_t row = hist_row(e, spe);
+#pragma unroll
+            for (int j = 0; j < WPT; j++)
+                if (active[j])
+                {
+                    if (e > 0)
+                        for (int s = 0; s < spe; s++)
+                        {
+                            bool wall;
+                            int ph;
+                            walker_step<BC, 1>(im, p[j], seed[j], wall, ph);
+                            c[j] += wall ? 1u : 0u;
+                        }
+                    atomicAdd(H + row + c[j], 1u);
+                }
+        }
+    }
+}
+
+// Echo sums from the histograms: out[e][o] = sum_c H[e][c] V_o[c] for 32 outputs o per image, the
+// 16 candidates' energies V_r[c] = round(f_r^c 2^57) and their derivative terms
+// V_16+r[c] = c * (round(f_r^(c-1) 2^57) >> dshift) -- the same integers the candidate walk adds up
+// walker by walker, so both paths return identical sums. Exact arithmetic: V is split into 32-bit
+// halves and each half's products h * V_half are summed in u64 (h * 2^32 summed over fewer than
+// 2^31 walkers stays below 2^63); the two sums are stored as the accumulators' lo / hi words.
+// A CTA computes kEvRows echoes x 32 outputs; thread t owns output t % 32 for kEvRows / 8 echoes.
+// Histogram counts and candidate values are staged through shared memory kEvChunk counts at a time.
+constexpr int kEvRows = 32, kEvChunk = 64, kEvThreads = 256;
+constexpr int kEvRowsPerThread = kEvRows / (kEvThreads / 32);
+
+__global__ void __launch_bounds__(kEvThreads) batch_eval_kernel(BatchLaunch L, int row_blocks)
+{
+    // [c][echo] and [c][output]; one padding column keeps the staging stores (consecutive threads,
+    // consecutive c) off a single bank
+    __shared__ unsigned sh[kEvChunk][kEvRows + 1];
+    __shared__ unsigned long long sv[kEvChunk][2 * kCand + 1];
+    const int img_i = blockIdx.x / row_blocks;
+    const int e0 = (blockIdx.x % row_blocks) * kEvRows;
+    const BatchImage img = L.images[img_i];
+    const unsigned *H = L.hist + img.hist0;
+    const ulonglong2 *tab2 = reinterpret_cast<const ulonglong2 *>(L.tab + img.tab0);
+    const int spe = L.steps_per_echo;
+    const int e_last = min(e0 + kEvRows - 1, L.n_echoes);
+    const int64_t cmax = (int64_t)spe * e_last; // largest count any of these rows holds
+    const int o = threadIdx.x & 31;
+    const int rg = (threadIdx.x >> 5) * kEvRowsPerThread;
+    unsigned long long lo[kEvRowsPerThread], hi[kEvRowsPerThread];
+#pragma unroll
+    for (int k = 0; k < kEvRowsPerThread; k++) lo[k] = hi[k] = 0;
+    for (int64_t c0 = 0; c0 <= cmax; c0 += kEvChunk)
+    {
+        for (int k = threadIdx.x; k < kEvChunk * kEvRows; k += kEvThreads)
+        {
+            const int r = k / kEvChunk, cc = k % kEvChunk; // consecutive threads read consecutive counts
+            const int e = e0 + r;
+            const int64_t c = c0 + cc;
+            sh[cc][r] = (e <= L.n_echoes && c <= (int64_t)spe * e) ? H[hist_row(e, spe) + c] : 0u;
+        }
+        for (int k = threadIdx.x; k < kEvChunk * kCand / 2; k += kEvThreads)
+        {
+            const int q = k / kEvChunk, cc = k % kEvChunk; // candidate pair q, count c0 + cc
+            const int64_t c = c0 + cc;
+            ulonglong2 t = make_ulonglong2(0, 0), tm = make_ulonglong2(0, 0);
+            if (c < L.tstride) t = tab2[(size_t)q * L.tstride + c];
+            if (c >= 1 && c < L.tstride) tm = tab2[(size_t)q * L.tstride + c - 1];
+            sv[cc][2 * q] = t.x;
+            sv[cc][2 * q + 1] = t.y;
+            sv[cc][kCand + 2 * q] = (unsigned long long)c * (tm.x >> L.dshift);
+            sv[cc][kCand + 2 * q + 1] = (unsigned long long)c * (tm.y >> L.dshift);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int cc = 0; cc < kEvChunk; cc++)
+        {
+            const unsigned long long v = sv[cc][o];
+            const unsigned vl = (unsigned)v, vh = (unsigned)(v >> 32);
+#pragma unroll
+            for (int k = 0; k < kEvRowsPerThread; k++)
+            {
+                const unsigned h = sh[cc][rg + k];
+                lo[k] += (unsigned long long)h * vl;
+                hi[k] += (unsigned long long)h * vh;
+            }
+        }
+        __syncthreads();
+    }
+    if (o >= kCand && !L.deriv) return;
+    unsigned long long *acc = L.acc + img.acc0;
+#pragma unroll
+    for (int k = 0; k < kEvRowsPerThread; k++)
+    {
+        const int e = e0 + rg + k;
+        if (e > L.n_echoes) break;
+        unsigned long long *a = acc + ((size_t)e * kCand + (o & (kCand - 1))) * 4 + (o >= kCand ? 2 : 0);
+        a[0] = lo[k];
+        a[1] = hi[k];
+    }
+}
+
 // Energy tables for every (image, candidate): round(f^c 2^57), f^c the FP64 repeated product. The
 // walk derives the derivative c f^(c-1) from the same table (c * (T[c-1] >> dshift), exact integer
 // arithmetic), so only one table per candidate competes for L2. One thread per (image, candidate).
@@ -302,9 +453,15 @@ struct rwnmr_batch
     unsigned long long *h_acc = nullptr;
     unsigned *h_status = nullptr;
     cudaGraphExec_t graph = nullptr;
-    int graph_key[5] = {0, 0, 0, 0, 0};
+    int graph_key[7] = {0, 0, 0, 0, 0, 0, 0};
+    // per-echo collision histograms of the last histogram walk, valid for hist_key
+    unsigned *d_hist = nullptr;
+    size_t hist_alloc = 0; // u32 words allocated
+    bool hist_valid = false;
+    int hist_key[3] = {0, 0, 0}; // n_echoes, steps_per_echo, bc
+    double hist_ms = 0.0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    double last_ms = 0.0;
+    double last_ms = 0.0, last_eval_ms = 0.0;
     int64_t launches = 0;
     int tuned_block = 0, tuned_wpt = 0;
     int sms = 0;
@@ -325,6 +482,10 @@ struct rwnmr_batch
         d_tab = d_acc = nullptr;
         d_counter = d_status = nullptr;
         d_f = nullptr;
+        if (d_hist) cudaFree(d_hist);
+        d_hist = nullptr;
+        hist_alloc = 0;
+        hist_valid = false;
         if (h_f) cudaFreeHost(h_f);
         if (h_acc) cudaFreeHost(h_acc);
         if (h_status) cudaFreeHost(h_status);
@@ -374,6 +535,7 @@ rwnmr_status upload(rwnmr_batch *b, int n_echoes, int spe)
         off += b->h_blocks[k].size();
         b->images[k].tab0 = (int64_t)k * kCand * tstride;
         b->images[k].acc0 = (int64_t)k * (n_echoes + 1) * kCand * 4;
+        b->images[k].hist0 = (int64_t)k * hist_words(n_echoes, spe);
         b->images[k].u_shift = us;
     }
     if (nw)
@@ -423,6 +585,42 @@ rwnmr_status build_items(rwnmr_batch *b, int block)
     return RWNMR_OK;
 }
 
+BatchLaunch launch_args(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
+{
+    const int ni = (int)b->images.size();
+    BatchLaunch L{};
+    L.images = b->d_images;
+    L.items = b->d_items;
+    L.n_items = b->n_items;
+    L.n_echoes = p->n_echoes;
+    L.steps_per_echo = p->steps_per_echo;
+    L.bc = p->bc;
+    L.deriv = p->derivatives ? 1 : 0;
+    L.tstride = p->n_echoes * p->steps_per_echo + 1;
+    L.dshift = ni ? kScaleBits - b->images[0].u_shift : 0;
+    L.tab = b->d_tab;
+    L.acc = b->d_acc;
+    L.x0 = b->d_x;
+    L.y0 = b->d_y;
+    L.z0 = b->d_z;
+    L.seed0 = b->d_seed;
+    L.counter = b->d_counter;
+    L.status = b->d_status;
+    L.hist = b->d_hist;
+    return L;
+}
+
+// Launches kern over the work queue with as many resident CTAs as fit on the GPU.
+template <typename K>
+void launch_persistent(rwnmr_batch *b, K kern, const BatchLaunch &L, int block, size_t smem)
+{
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
+    const int grid = std::max(1, std::min(b->n_items, std::max(1, per_sm) * b->sms));
+    kern<<<grid, block, smem, b->stream>>>(L);
+}
+
+// Candidate walk: tables -> walk (every candidate's sums, walker by walker) -> copy-out.
 cudaError_t enqueue(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block, int wpt)
 {
     const int ni = (int)b->images.size();
@@ -434,35 +632,12 @@ cudaError_t enqueue(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block,
     if ((e = cudaMemsetAsync(b->d_acc, 0, b->acc_words * 8, b->stream))) return e;
     if ((e = cudaMemsetAsync(b->d_counter, 0, 4, b->stream))) return e;
     if ((e = cudaMemsetAsync(b->d_status, 0, 4, b->stream))) return e;
-    BatchLaunch L{};
-    L.images = b->d_images;
-    L.items = b->d_items;
-    L.n_items = b->n_items;
-    L.n_echoes = p->n_echoes;
-    L.steps_per_echo = p->steps_per_echo;
-    L.bc = p->bc;
-    L.deriv = p->derivatives ? 1 : 0;
-    L.tstride = tstride;
-    L.dshift = ni ? kScaleBits - b->images[0].u_shift : 0;
-    L.tab = b->d_tab;
-    L.acc = b->d_acc;
-    L.x0 = b->d_x;
-    L.y0 = b->d_y;
-    L.z0 = b->d_z;
-    L.seed0 = b->d_seed;
-    L.counter = b->d_counter;
-    L.status = b->d_status;
+    const BatchLaunch L = launch_args(b, p);
     const size_t smem = (size_t)kWin * kCand * 4 * 8;
-    int per_sm = 1;
-    auto occ = [&](auto kern) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
-        const int grid = std::max(1, std::min(b->n_items, std::max(1, per_sm) * b->sms));
-        kern<<<grid, block, smem, b->stream>>>(L);
-    };
     auto by_wpt = [&](auto bcc) {
         constexpr int BC = decltype(bcc)::value;
-        if (wpt == 2) occ(batch_cpmg_kernel<BC, 2>);
-        else occ(batch_cpmg_kernel<BC, 1>);
+        if (wpt == 2) launch_persistent(b, batch_cpmg_kernel<BC, 2>, L, block, smem);
+        else launch_persistent(b, batch_cpmg_kernel<BC, 1>, L, block, smem);
     };
     if (p->bc == RWNMR_BC_PERIODIC) by_wpt(std::integral_constant<int, BC_PERIODIC>{});
     else if (p->bc == RWNMR_BC_MIRROR) by_wpt(std::integral_constant<int, BC_MIRROR>{});
@@ -470,6 +645,94 @@ cudaError_t enqueue(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block,
     if ((e = cudaGetLastError())) return e;
     if ((e = cudaMemcpyAsync(b->h_acc, b->d_acc, b->acc_words * 8, cudaMemcpyDeviceToHost, b->stream))) return e;
     return cudaMemcpyAsync(b->h_status, b->d_status, 4, cudaMemcpyDeviceToHost, b->stream);
+}
+
+// Histogram evaluation: tables -> sums from the stored histograms -> copy-out (no walk).
+cudaError_t enqueue_eval(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
+{
+    const int ni = (int)b->images.size();
+    const int tstride = p->n_echoes * p->steps_per_echo + 1;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(b->d_f, b->h_f, (size_t)ni * kCand * 8, cudaMemcpyHostToDevice, b->stream))) return e;
+    batch_tables_kernel<<<(ni * kCand + 127) / 128, 128, 0, b->stream>>>(b->d_f, ni, tstride, b->d_tab);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = cudaMemsetAsync(b->d_acc, 0, b->acc_words * 8, b->stream))) return e;
+    const BatchLaunch L = launch_args(b, p);
+    const int row_blocks = (p->n_echoes + 1 + kEvRows - 1) / kEvRows;
+    batch_eval_kernel<<<ni * row_blocks, kEvThreads, 0, b->stream>>>(L, row_blocks);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = cudaMemcpyAsync(b->h_acc, b->d_acc, b->acc_words * 8, cudaMemcpyDeviceToHost, b->stream))) return e;
+    return cudaMemcpyAsync(b->h_status, b->d_status, 4, cudaMemcpyDeviceToHost, b->stream);
+}
+
+size_t hist_bytes(const rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
+{
+    return b->images.size() * (size_t)hist_words(p->n_echoes, p->steps_per_echo) * 4;
+}
+
+// Method of a call: histograms unless asked otherwise or they would take more than half the free
+// device memory (then every call walks its candidates).
+int resolve_method(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
+{
+    if (p->method == RWNMR_BATCH_CANDIDATE_WALK) return RWNMR_BATCH_CANDIDATE_WALK;
+    if (p->method == RWNMR_BATCH_HISTOGRAMS) return RWNMR_BATCH_HISTOGRAMS;
+    if (b->hist_valid && b->hist_key[0] == p->n_echoes && b->hist_key[1] == p->steps_per_echo && b->hist_key[2] == p->bc)
+        return RWNMR_BATCH_HISTOGRAMS;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return RWNMR_BATCH_CANDIDATE_WALK;
+    const size_t need = hist_bytes(b, p);
+    return need <= (free_b + b->hist_alloc * 4) / 2 ? RWNMR_BATCH_HISTOGRAMS : RWNMR_BATCH_CANDIDATE_WALK;
+}
+
+// Runs the histogram walk unless the stored histograms already belong to this walk (same echoes,
+// steps per echo and boundary condition; images and walkers are fixed once uploaded).
+rwnmr_status histogram_walk(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block, int wpt, bool force,
+                            bool *walked)
+{
+    *walked = false;
+    if (!force && b->hist_valid && b->hist_key[0] == p->n_echoes && b->hist_key[1] == p->steps_per_echo &&
+        b->hist_key[2] == p->bc)
+        return RWNMR_OK;
+    *walked = true;
+    const size_t words = b->images.size() * (size_t)hist_words(p->n_echoes, p->steps_per_echo);
+    if (b->hist_alloc < words)
+    {
+        if (b->d_hist) cudaFree(b->d_hist);
+        b->d_hist = nullptr;
+        b->hist_alloc = 0;
+        BT_CUDA(b, cudaMalloc(&b->d_hist, std::max<size_t>(words, 1) * 4), "collision histograms");
+        b->hist_alloc = words;
+        if (b->graph) cudaGraphExecDestroy(b->graph); // the evaluation graph holds the old pointer
+        b->graph = nullptr;
+    }
+    b->hist_valid = false;
+    BT_CUDA(b, cudaMemsetAsync(b->d_hist, 0, words * 4, b->stream), "histogram reset");
+    BT_CUDA(b, cudaMemsetAsync(b->d_counter, 0, 4, b->stream), "histogram walk");
+    BT_CUDA(b, cudaMemsetAsync(b->d_status, 0, 4, b->stream), "histogram walk");
+    BT_CUDA(b, cudaEventRecord(b->ev0, b->stream), "event");
+    const BatchLaunch L = launch_args(b, p);
+    auto by_wpt = [&](auto bcc) {
+        constexpr int BC = decltype(bcc)::value;
+        if (wpt == 2) launch_persistent(b, batch_hist_kernel<BC, 2>, L, block, 0);
+        else launch_persistent(b, batch_hist_kernel<BC, 1>, L, block, 0);
+    };
+    if (p->bc == RWNMR_BC_PERIODIC) by_wpt(std::integral_constant<int, BC_PERIODIC>{});
+    else if (p->bc == RWNMR_BC_MIRROR) by_wpt(std::integral_constant<int, BC_MIRROR>{});
+    else by_wpt(std::integral_constant<int, BC_NOFLUX>{});
+    BT_CUDA(b, cudaGetLastError(), "histogram walk");
+    BT_CUDA(b, cudaEventRecord(b->ev1, b->stream), "event");
+    BT_CUDA(b, cudaMemcpyAsync(b->h_status, b->d_status, 4, cudaMemcpyDeviceToHost, b->stream), "histogram walk");
+    BT_CUDA(b, cudaStreamSynchronize(b->stream), "histogram walk");
+    b->launches += 1;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    b->hist_ms = ms;
+    if (*b->h_status & kStatusBadStart) return put(b->err, RWNMR_ERR_INVALID, "a walker starts outside its image");
+    b->hist_key[0] = p->n_echoes;
+    b->hist_key[1] = p->steps_per_echo;
+    b->hist_key[2] = p->bc;
+    b->hist_valid = true;
+    return RWNMR_OK;
 }
 
 rwnmr_status check_params(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
@@ -485,6 +748,8 @@ rwnmr_status check_params(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
         return put(b->err, RWNMR_ERR_INVALID, "threads_per_block must be a multiple of 32 in 64..512");
     if (p->walkers_per_thread < 0 || p->walkers_per_thread > 2)
         return put(b->err, RWNMR_ERR_INVALID, "walkers_per_thread must be 0 (tuned), 1 or 2");
+    if (p->method < RWNMR_BATCH_AUTO || p->method > RWNMR_BATCH_CANDIDATE_WALK)
+        return put(b->err, RWNMR_ERR_INVALID, "unknown batch method");
     return RWNMR_OK;
 }
 } // namespace
@@ -591,9 +856,19 @@ rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, 
     const int block = p->threads_per_block ? p->threads_per_block : (b->tuned_block ? b->tuned_block : 256);
     const int wpt = p->walkers_per_thread ? p->walkers_per_thread : (b->tuned_wpt ? b->tuned_wpt : 1);
     if ((st = build_items(b, block * wpt)) != RWNMR_OK) return st;
+    const int method = resolve_method(b, p);
+    double walk_ms = 0.0;
+    if (method == RWNMR_BATCH_HISTOGRAMS)
+    {
+        bool walked = false;
+        if ((st = histogram_walk(b, p, block, wpt, false, &walked)) != RWNMR_OK) return st;
+        walk_ms = walked ? b->hist_ms : 0.0;
+    }
     for (int k = 0; k < ni; k++)
         for (int r = 0; r < kCand; r++) b->h_f[k * kCand + r] = r < R ? dfactor[k * R + r] : 1.0;
-    const int key[6] = {p->n_echoes, p->steps_per_echo, p->bc, p->derivatives ? 1 : 0, block, wpt};
+    const bool hist = method == RWNMR_BATCH_HISTOGRAMS;
+    const int key[7] = {p->n_echoes, p->steps_per_echo, p->bc, p->derivatives ? 1 : 0, hist ? 0 : block,
+                        hist ? 0 : wpt, method};
     BT_CUDA(b, cudaEventRecord(b->ev0, b->stream), "event");
     if (p->use_graph)
     {
@@ -603,7 +878,7 @@ rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, 
             b->graph = nullptr;
             cudaGraph_t g;
             BT_CUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
-            cudaError_t ce = enqueue(b, p, block, wpt);
+            cudaError_t ce = hist ? enqueue_eval(b, p) : enqueue(b, p, block, wpt);
             cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
             BT_CUDA(b, ce, "graph capture");
             BT_CUDA(b, ee, "graph capture");
@@ -615,13 +890,14 @@ rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, 
         BT_CUDA(b, cudaGraphLaunch(b->graph, b->stream), "graph launch");
     }
     else
-        BT_CUDA(b, enqueue(b, p, block, wpt), "batch launch");
+        BT_CUDA(b, hist ? enqueue_eval(b, p) : enqueue(b, p, block, wpt), "batch launch");
     b->launches += 2;
     BT_CUDA(b, cudaEventRecord(b->ev1, b->stream), "event");
     BT_CUDA(b, cudaStreamSynchronize(b->stream), "batch walk");
     float ms = 0.f;
     cudaEventElapsedTime(&ms, b->ev0, b->ev1);
-    b->last_ms = ms;
+    b->last_ms = ms + walk_ms; // this call's GPU time, its histogram walk included
+    b->last_eval_ms = hist ? ms : 0.0;
     if (*b->h_status & kStatusBadStart) return put(b->err, RWNMR_ERR_INVALID, "a walker starts outside its image");
     const int E1 = p->n_echoes + 1;
     for (int k = 0; k < ni; k++)
@@ -650,15 +926,38 @@ rwnmr_status rwnmr_batch_autotune(rwnmr_batch *b, const rwnmr_batch_cpmg_params 
     if (st != RWNMR_OK) return st;
     const int ni = (int)b->images.size();
     std::vector<double> f((size_t)ni * p->n_candidates, 0.999);
+    cudaSetDevice(b->device);
+    if ((st = upload(b, p->n_echoes, p->steps_per_echo)) != RWNMR_OK) return st;
+    const bool hist = resolve_method(b, p) == RWNMR_BATCH_HISTOGRAMS;
     double best = 1e30;
     int arg = 256, arg_w = 1;
     for (int w : {1, 2})
         for (int t : {128, 256, 512})
         {
+            if (hist)
+            {
+                // the walk the method runs: the histogram walk (timed twice, the faster kept)
+                bool walked = false;
+                double ms = 1e30;
+                for (int rep = 0; rep < 2; rep++)
+                {
+                    if ((st = build_items(b, t * w)) != RWNMR_OK) return st;
+                    if ((st = histogram_walk(b, p, t, w, true, &walked)) != RWNMR_OK) return st;
+                    ms = std::min(ms, b->hist_ms);
+                }
+                if (ms < best)
+                {
+                    best = ms;
+                    arg = t;
+                    arg_w = w;
+                }
+                continue;
+            }
             rwnmr_batch_cpmg_params q = *p;
             q.threads_per_block = t;
             q.walkers_per_thread = w;
             q.use_graph = 0;
+            q.method = RWNMR_BATCH_CANDIDATE_WALK;
             if ((st = rwnmr_batch_cpmg(b, &q, f.data(), nullptr, nullptr)) != RWNMR_OK) return st;
             if ((st = rwnmr_batch_cpmg(b, &q, f.data(), nullptr, nullptr)) != RWNMR_OK) return st;
             if (b->last_ms < best)
@@ -668,6 +967,8 @@ rwnmr_status rwnmr_batch_autotune(rwnmr_batch *b, const rwnmr_batch_cpmg_params 
                 arg_w = w;
             }
         }
+    // the sweep's histograms are dropped: the next call walks (and times) its own
+    b->hist_valid = false;
     b->tuned_block = arg;
     b->tuned_wpt = arg_w;
     if (best_threads) *best_threads = arg;
@@ -675,5 +976,24 @@ rwnmr_status rwnmr_batch_autotune(rwnmr_batch *b, const rwnmr_batch_cpmg_params 
     if (best_ms) *best_ms = best;
     return RWNMR_OK;
 }
+
+rwnmr_status rwnmr_batch_collision_histogram(rwnmr_batch *b, int32_t image, int32_t echo, uint32_t *counts,
+                                             int32_t *n_counts)
+{
+    if (!b) return RWNMR_ERR_INVALID;
+    if (!b->hist_valid) return put(b->err, RWNMR_ERR_STATE, "no histogram walk has run");
+    if (image < 0 || image >= (int)b->images.size() || echo < 0 || echo > b->hist_key[0])
+        return put(b->err, RWNMR_ERR_INVALID, "image or echo out of range");
+    const int spe = b->hist_key[1];
+    const int64_t n = (int64_t)spe * echo + 1;
+    if (n_counts) *n_counts = (int32_t)n;
+    if (!counts) return RWNMR_OK;
+    cudaSetDevice(b->device);
+    BT_CUDA(b, cudaMemcpy(counts, b->d_hist + b->images[image].hist0 + hist_row(echo, spe), (size_t)n * 4,
+                          cudaMemcpyDeviceToHost), "histogram download");
+    return RWNMR_OK;
+}
+
+double rwnmr_batch_histogram_walk_ms(const rwnmr_batch *b) { return b ? b->hist_ms : 0.0; }
 
 } // extern "C"

@@ -37,7 +37,8 @@ EXPORTS = [
     "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_map_continue", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
     "rwnmr_cpmg_run_noalloc", "rwnmr_batch_create", "rwnmr_batch_destroy", "rwnmr_batch_last_error",
     "rwnmr_batch_last_kernel_ms", "rwnmr_batch_launch_count", "rwnmr_batch_add_image", "rwnmr_batch_cpmg",
-    "rwnmr_batch_autotune", "rwnmr_field_set_uniform", "rwnmr_field_upload", "rwnmr_field_clear",
+    "rwnmr_batch_autotune", "rwnmr_batch_collision_histogram", "rwnmr_batch_histogram_walk_ms",
+    "rwnmr_field_set_uniform", "rwnmr_field_upload", "rwnmr_field_clear",
     "rwnmr_cpmg_field_run", "rwnmr_walkers_set_dfactor",
 ]
 
@@ -103,6 +104,8 @@ def load_library(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.rwnmr_batch_last_kernel_ms.argtypes = [_vp]
         lib.rwnmr_batch_launch_count.restype = ctypes.c_int64
         lib.rwnmr_batch_launch_count.argtypes = [_vp]
+        lib.rwnmr_batch_histogram_walk_ms.restype = ctypes.c_double
+        lib.rwnmr_batch_histogram_walk_ms.argtypes = [_vp]
         lib.rwnmr_batch_destroy.argtypes = [_vp]
         for name in EXPORTS:
             getattr(lib, name)  # raises AttributeError if a declared symbol is missing
@@ -302,7 +305,10 @@ class BatchParams(ctypes.Structure):
     _fields_ = [("bc", ctypes.c_int32), ("steps_per_echo", ctypes.c_int32), ("n_echoes", ctypes.c_int32),
                 ("n_candidates", ctypes.c_int32), ("derivatives", ctypes.c_int32),
                 ("threads_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32),
-                ("walkers_per_thread", ctypes.c_int32)]
+                ("walkers_per_thread", ctypes.c_int32), ("method", ctypes.c_int32)]
+
+
+BATCH_METHOD = {"auto": 0, "histograms": 1, "walk": 2}
 
 
 class Batch:
@@ -345,21 +351,26 @@ class Batch:
         return idx.value
 
     def cpmg(self, dfactor, n_echoes: int, steps_per_echo: int, derivatives: bool = True, bc: str = "noflux",
-             threads_per_block: int = 0, use_graph: bool = True, walkers_per_thread: int = 0):
+             threads_per_block: int = 0, use_graph: bool = True, walkers_per_thread: int = 0, method: str = "auto"):
+        """Echo sums [image][candidate][echo] (and derivatives) for dfactor [image][candidate].
+        method "histograms" walks once per (n_echoes, steps_per_echo, bc) and evaluates every later
+        call from the stored per-echo collision histograms; "walk" walks on every call; "auto" picks
+        histograms when they fit in half the free device memory. Both give identical sums."""
         f = np.ascontiguousarray(dfactor, np.float64)
         if f.ndim == 1:
             f = f[:, None]
         R = f.shape[1]
         prm = BatchParams(BC[bc], int(steps_per_echo), int(n_echoes), R, int(bool(derivatives)),
-                          int(threads_per_block), int(bool(use_graph)), int(walkers_per_thread))
+                          int(threads_per_block), int(bool(use_graph)), int(walkers_per_thread), BATCH_METHOD[method])
         echo = np.zeros((self.n_images, R, n_echoes + 1))
         decho = np.zeros_like(echo) if derivatives else None
         self._check(self.lib.rwnmr_batch_cpmg(self.b, ctypes.byref(prm), _p(f), _p(echo), _p(decho)))
         return echo, decho
 
     def autotune(self, n_echoes: int, steps_per_echo: int, n_candidates: int = 16, derivatives: bool = True,
-                 bc: str = "noflux"):
-        prm = BatchParams(BC[bc], int(steps_per_echo), int(n_echoes), int(n_candidates), int(bool(derivatives)), 0, 0, 0)
+                 bc: str = "noflux", method: str = "auto"):
+        prm = BatchParams(BC[bc], int(steps_per_echo), int(n_echoes), int(n_candidates), int(bool(derivatives)), 0, 0, 0,
+                          BATCH_METHOD[method])
         t = ctypes.c_int32()
         wpt = ctypes.c_int32()
         ms = ctypes.c_double()
@@ -374,6 +385,18 @@ class Batch:
     @property
     def launch_count(self) -> int:
         return int(self.lib.rwnmr_batch_launch_count(self.b))
+
+    @property
+    def histogram_walk_ms(self) -> float:
+        return float(self.lib.rwnmr_batch_histogram_walk_ms(self.b))
+
+    def collision_histogram(self, image: int, echo: int) -> np.ndarray:
+        """Walkers of `image` per collision count after `echo` (from the last histogram walk)."""
+        n = ctypes.c_int32()
+        self._check(self.lib.rwnmr_batch_collision_histogram(self.b, int(image), int(echo), None, ctypes.byref(n)))
+        out = np.zeros(n.value, np.uint32)
+        self._check(self.lib.rwnmr_batch_collision_histogram(self.b, int(image), int(echo), _p(out), ctypes.byref(n)))
+        return out
 
 
 def fx_to_float(limbs) -> np.ndarray:

@@ -1,6 +1,7 @@
 """Batched multi-image walk with relaxivity candidates: every (image, candidate) echo train
 against the single-image engine on the same walkers, derivatives against the seed-replay
-adjoint, graph replay and autotuning."""
+adjoint, graph replay and autotuning; the per-echo collision histograms against the oracle's
+per-walker collision counts, and histogram evaluation against the candidate walk (identical sums)."""
 import numpy as np
 import pytest
 
@@ -23,8 +24,9 @@ def make_images(n_images=5, seed=0):
     return out
 
 
-@pytest.mark.parametrize("bc", ["noflux", "periodic"])
-def test_batch_matches_single_image_engine(bc):
+@pytest.mark.parametrize("bc,method", [("noflux", "walk"), ("periodic", "walk"), ("noflux", "histograms"),
+                                       ("mirror", "histograms")])
+def test_batch_matches_single_image_engine(bc, method):
     imgs = make_images()
     n_echoes, spe = 40, 3
     rng = np.random.default_rng(1)
@@ -33,12 +35,13 @@ def test_batch_matches_single_image_engine(bc):
     b = Batch(0)
     for lab, blocks, w in imgs:
         b.add_image(blocks, lab.shape, *w)
-    echo, decho = b.cpmg(f, n_echoes, spe, derivatives=True, bc=bc)
-    echo2, decho2 = b.cpmg(f, n_echoes, spe, derivatives=True, bc=bc, use_graph=False)
+    echo, decho = b.cpmg(f, n_echoes, spe, derivatives=True, bc=bc, method=method)
+    echo2, decho2 = b.cpmg(f, n_echoes, spe, derivatives=True, bc=bc, use_graph=False, method=method)
     assert np.array_equal(echo, echo2) and np.array_equal(decho, decho2)
     # launch shape and walkers per thread do not change the exact sums
     for t, wpt in ((128, 2), (512, 1), (256, 2)):
-        echo3, decho3 = b.cpmg(f, n_echoes, spe, derivatives=True, bc=bc, threads_per_block=t, walkers_per_thread=wpt)
+        echo3, decho3 = b.cpmg(f, n_echoes, spe, derivatives=True, bc=bc, threads_per_block=t, walkers_per_thread=wpt,
+                               method="walk")
         assert np.array_equal(echo3, echo) and np.array_equal(decho3, decho)
     eng = Engine(0)
     for k, (lab, blocks, w) in enumerate(imgs):
@@ -66,4 +69,54 @@ def test_batch_autotune_and_fewer_candidates():
     assert echo.shape == (3, 2, 21)
     full, _ = b.cpmg(np.concatenate([f, np.ones((3, 14))], 1), 20, 2, derivatives=False)
     assert np.array_equal(full[:, :2], echo)
+    b.close()
+
+
+@pytest.mark.parametrize("bc", ["noflux", "periodic", "mirror"])
+def test_histograms_and_candidate_walk_agree_exactly(bc):
+    """Sums evaluated from the per-echo collision histograms equal the candidate walk's sums bit for
+    bit; a second candidate population is evaluated from the stored histograms without a walk."""
+    imgs = make_images(4, seed=7)
+    b = Batch(0)
+    for lab, blocks, w in imgs:
+        b.add_image(blocks, lab.shape, *w)
+    rng = np.random.default_rng(3)
+    for n_echoes, spe in ((30, 3), (17, 1), (9, 5)):
+        f = dfactor(rng.uniform(2.0, 50.0, (4, 16)))
+        eh, dh = b.cpmg(f, n_echoes, spe, bc=bc, method="histograms")
+        assert b.histogram_walk_ms > 0
+        ew, dw = b.cpmg(f, n_echoes, spe, bc=bc, method="walk")
+        assert np.array_equal(eh, ew) and np.array_equal(dh, dw)
+        f2 = dfactor(rng.uniform(2.0, 50.0, (4, 16)))
+        launches = b.launch_count
+        eh2, dh2 = b.cpmg(f2, n_echoes, spe, bc=bc, method="histograms")
+        assert b.launch_count - launches == 2  # tables and evaluation: no walk
+        ew2, dw2 = b.cpmg(f2, n_echoes, spe, bc=bc, method="walk")
+        assert np.array_equal(eh2, ew2) and np.array_equal(dh2, dw2)
+        e3, d3 = b.cpmg(f2[:, :5], n_echoes, spe, derivatives=False, bc=bc, method="histograms")
+        assert d3 is None and np.array_equal(e3, eh2[:, :5])
+    b.close()
+
+
+def test_collision_histograms_match_oracle(oracle):
+    """Row e of an image's histogram counts that image's walkers by their collision count after
+    echo e, exactly as the oracle's per-walker counts after e echoes give."""
+    imgs = make_images(3, seed=9)
+    b = Batch(0)
+    for lab, blocks, w in imgs:
+        b.add_image(blocks, lab.shape, *w)
+    spe, n_echoes = 2, 25
+    b.cpmg(np.full((3, 1), 0.99), n_echoes, spe, derivatives=False, method="histograms")
+    for k, (lab, blocks, w) in enumerate(imgs):
+        n = len(w[0])
+        for e in (0, 1, 7, n_echoes):
+            h = b.collision_histogram(k, e)
+            assert len(h) == spe * e + 1 and int(h.sum()) == n
+            if e == 0 or n == 0:
+                assert h[0] == n
+                continue
+            coll = oracle.cpmg(lab, w, e, spe, 0.99, threads=4)["collf"][:, 0]
+            assert np.array_equal(h, np.bincount(coll, minlength=spe * e + 1))
+    with pytest.raises(Exception):
+        b.collision_histogram(0, n_echoes + 1)
     b.close()
