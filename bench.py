@@ -296,7 +296,7 @@ def run_fit_batch(args):
     nwalk = np.array([len(im[2][0]) for im in imgs])
     # tune on a walk long enough for the collision counts (and so the table gathers) to spread as in
     # the fit; the sweep's GPU time is reported separately from the fit's
-    tuned, tuned_wpt, tune_ms = b.autotune(min(echoes, 1000), spe, 16)
+    tuned, tuned_wpt, tune_ms = b.autotune(min(echoes, 1000), spe, 16, method=args.batch_method)
     hidden = rng.uniform(2.0, 50.0, n_img)
     fh = np.ones((n_img, 16))
     fh[:, 0] = decrease_factor(hidden)
@@ -306,8 +306,8 @@ def run_fit_batch(args):
     bulk = np.exp(-echo_times(echoes, spe, 1.0 / 15.0) / t2b)
     targets = echo[:, 0] / nwalk[:, None] * bulk + rng.normal(0.0, 1e-3, (n_img, echoes + 1))
     rho0 = rng.uniform(2.0, 50.0, (n_img, 16))
-    fit = fit_rho_batch(b, targets, nwalk, echoes, spe, t2b, rho0, iters=args.fit_iters)
-    hist_walk_s = b.histogram_walk_ms * 1e-3
+    fit = fit_rho_batch(b, targets, nwalk, echoes, spe, t2b, rho0, iters=args.fit_iters, method=args.batch_method)
+    hist_walk_s = b.histogram_walk_ms * 1e-3 if args.batch_method != "walk" else 0.0
     steps_per_pass = int(nwalk.sum()) * echoes * spe
     # plain per-image CPMG: one walk per image per GA evaluation
     eng = Engine(0)
@@ -337,10 +337,14 @@ def run_fit_batch(args):
                        "walker_steps_per_pass": steps_per_pass, "autotuned_threads": tuned, "autotuned_walkers_per_thread": tuned_wpt,
                        "autotune_best_walk_ms": tune_ms,
                        "setup_seconds": setup_s},
-            "batched_fit": {"gpu_seconds": fit["gpu_seconds"], "passes": fit["walks"], "method": "histograms",
+            "batched_fit": {"gpu_seconds": fit["gpu_seconds"], "passes": fit["walks"],
+                            "method": "walk" if args.batch_method == "walk" else "histograms",
                             "histogram_walk_seconds": hist_walk_s,
-                            "histogram_walk_walker_steps_per_s": steps_per_pass / max(hist_walk_s, 1e-12),
-                            "evaluation_ms_per_pass": (fit["gpu_seconds"] - hist_walk_s) * 1e3 / fit["walks"],
+                            "histogram_walk_walker_steps_per_s": steps_per_pass / hist_walk_s if hist_walk_s else None,
+                            "evaluation_ms_per_pass": ((fit["gpu_seconds"] - hist_walk_s) * 1e3 / fit["walks"]
+                                                       if hist_walk_s else None),
+                            "candidate_walk_walker_steps_per_s": (None if hist_walk_s else
+                                                                  steps_per_pass * fit["walks"] / fit["gpu_seconds"]),
                             "max_abs_rho_error": float(np.max(np.abs(fit["rho"] - hidden))),
                             "median_abs_rho_error": float(np.median(np.abs(fit["rho"] - hidden)))},
             "per_image_cpmg_ga": {"gpu_seconds_estimate": ga_gpu, "plain_walk_gpu_seconds_all_images":
@@ -513,6 +517,8 @@ def main():
     ap.add_argument("--fit-iters", type=int, default=6)
     ap.add_argument("--echoes", type=int, default=0, help="rho-fit-batch: echo count override (profiling)")
     ap.add_argument("--images", type=int, default=0, help="rho-fit-batch: use the first N images (profiling)")
+    ap.add_argument("--batch-method", default="auto", choices=["auto", "histograms", "walk"],
+                    help="rho-fit-batch: histogram evaluation (auto) or a candidate walk per fit iteration")
     args = ap.parse_args()
     if args.workload.startswith("rho-fit-multiphase"):
         return run_fit_multiphase(args)

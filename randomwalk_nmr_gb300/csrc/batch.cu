@@ -76,6 +76,7 @@ struct BatchLaunch
     unsigned *counter;
     unsigned *status;
     unsigned *hist;                // collision histograms (histogram walk), see hist_row
+    uint2 *hist_range;             // [image][n_echoes + 1]: first and last non-zero count of each row
 };
 
 // Per-echo collision histograms: after echo e a walker has at most steps_per_echo * e collisions,
@@ -300,6 +301,29 @@ __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
     }
 }
 
+// First and last non-zero count of every histogram row ({1, 0} for an empty row), one warp per row,
+// so that the evaluation skips the stretches of counts no walker reached.
+__global__ void batch_range_kernel(BatchLaunch L, int n_images)
+{
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int64_t rows_per_image = L.n_echoes + 1;
+    if (row >= (int64_t)n_images * rows_per_image) return;
+    const int img_i = (int)(row / rows_per_image), e = (int)(row % rows_per_image);
+    const unsigned *h = L.hist + L.images[img_i].hist0 + hist_row(e, L.steps_per_echo);
+    const unsigned n = (unsigned)L.steps_per_echo * e + 1;
+    unsigned lo = 0xffffffffu, hi = 0;
+    for (unsigned c = lane; c < n; c += 32)
+        if (h[c])
+        {
+            lo = min(lo, c);
+            hi = c;
+        }
+    lo = __reduce_min_sync(FULLM, lo);
+    hi = __reduce_max_sync(FULLM, hi);
+    if (lane == 0) L.hist_range[row] = lo == 0xffffffffu ? make_uint2(1, 0) : make_uint2(lo, hi);
+}
+
 // Echo sums from the histograms: out[e][o] = sum_c H[e][c] V_o[c] for 32 outputs o per image, the
 // 16 candidates' energies V_r[c] = round(f_r^c 2^57) and their derivative terms
 // V_16+r[c] = c * (round(f_r^(c-1) 2^57) >> dshift) -- the same integers the candidate walk adds up
@@ -324,13 +348,27 @@ __global__ void __launch_bounds__(kEvThreads) batch_eval_kernel(BatchLaunch L, i
     const ulonglong2 *tab2 = reinterpret_cast<const ulonglong2 *>(L.tab + img.tab0);
     const int spe = L.steps_per_echo;
     const int e_last = min(e0 + kEvRows - 1, L.n_echoes);
-    const int64_t cmax = (int64_t)spe * e_last; // largest count any of these rows holds
+    // counts any of these rows holds: the union of their non-zero ranges
+    __shared__ unsigned s_lo, s_hi;
+    if (threadIdx.x < 32)
+    {
+        const int e = e0 + threadIdx.x;
+        const uint2 r = e <= e_last ? L.hist_range[(int64_t)img_i * (L.n_echoes + 1) + e] : make_uint2(0xffffffffu, 0);
+        const unsigned lo = __reduce_min_sync(FULLM, r.x), hi = __reduce_max_sync(FULLM, r.y);
+        if (threadIdx.x == 0)
+        {
+            s_lo = lo;
+            s_hi = hi;
+        }
+    }
+    __syncthreads();
+    const int64_t cmin = s_lo & ~(unsigned)(kEvChunk - 1), cmax = s_hi;
     const int o = threadIdx.x & 31;
     const int rg = (threadIdx.x >> 5) * kEvRowsPerThread;
     unsigned long long lo[kEvRowsPerThread], hi[kEvRowsPerThread];
 #pragma unroll
     for (int k = 0; k < kEvRowsPerThread; k++) lo[k] = hi[k] = 0;
-    for (int64_t c0 = 0; c0 <= cmax; c0 += kEvChunk)
+    for (int64_t c0 = cmin; c0 <= cmax; c0 += kEvChunk)
     {
         for (int k = threadIdx.x; k < kEvChunk * kEvRows; k += kEvThreads)
         {
@@ -456,7 +494,8 @@ struct rwnmr_batch
     int graph_key[7] = {0, 0, 0, 0, 0, 0, 0};
     // per-echo collision histograms of the last histogram walk, valid for hist_key
     unsigned *d_hist = nullptr;
-    size_t hist_alloc = 0; // u32 words allocated
+    uint2 *d_hist_range = nullptr;
+    size_t hist_alloc = 0, range_alloc = 0; // u32 words / rows allocated
     bool hist_valid = false;
     int hist_key[3] = {0, 0, 0}; // n_echoes, steps_per_echo, bc
     double hist_ms = 0.0;
@@ -483,8 +522,10 @@ struct rwnmr_batch
         d_counter = d_status = nullptr;
         d_f = nullptr;
         if (d_hist) cudaFree(d_hist);
+        if (d_hist_range) cudaFree(d_hist_range);
         d_hist = nullptr;
-        hist_alloc = 0;
+        d_hist_range = nullptr;
+        hist_alloc = range_alloc = 0;
         hist_valid = false;
         if (h_f) cudaFreeHost(h_f);
         if (h_acc) cudaFreeHost(h_acc);
@@ -607,6 +648,7 @@ BatchLaunch launch_args(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
     L.counter = b->d_counter;
     L.status = b->d_status;
     L.hist = b->d_hist;
+    L.hist_range = b->d_hist_range;
     return L;
 }
 
@@ -695,14 +737,19 @@ rwnmr_status histogram_walk(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, in
         return RWNMR_OK;
     *walked = true;
     const size_t words = b->images.size() * (size_t)hist_words(p->n_echoes, p->steps_per_echo);
-    if (b->hist_alloc < words)
+    const size_t rows = b->images.size() * (size_t)(p->n_echoes + 1);
+    if (b->hist_alloc < words || b->range_alloc < rows)
     {
         if (b->d_hist) cudaFree(b->d_hist);
+        if (b->d_hist_range) cudaFree(b->d_hist_range);
         b->d_hist = nullptr;
-        b->hist_alloc = 0;
+        b->d_hist_range = nullptr;
+        b->hist_alloc = b->range_alloc = 0;
         BT_CUDA(b, cudaMalloc(&b->d_hist, std::max<size_t>(words, 1) * 4), "collision histograms");
+        BT_CUDA(b, cudaMalloc(&b->d_hist_range, std::max<size_t>(rows, 1) * sizeof(uint2)), "collision histograms");
         b->hist_alloc = words;
-        if (b->graph) cudaGraphExecDestroy(b->graph); // the evaluation graph holds the old pointer
+        b->range_alloc = rows;
+        if (b->graph) cudaGraphExecDestroy(b->graph); // the evaluation graph holds the old pointers
         b->graph = nullptr;
     }
     b->hist_valid = false;
@@ -720,10 +767,15 @@ rwnmr_status histogram_walk(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, in
     else if (p->bc == RWNMR_BC_MIRROR) by_wpt(std::integral_constant<int, BC_MIRROR>{});
     else by_wpt(std::integral_constant<int, BC_NOFLUX>{});
     BT_CUDA(b, cudaGetLastError(), "histogram walk");
+    {
+        const int64_t threads = (int64_t)rows * 32;
+        batch_range_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, b->stream>>>(L, (int)b->images.size());
+        BT_CUDA(b, cudaGetLastError(), "histogram ranges");
+    }
     BT_CUDA(b, cudaEventRecord(b->ev1, b->stream), "event");
     BT_CUDA(b, cudaMemcpyAsync(b->h_status, b->d_status, 4, cudaMemcpyDeviceToHost, b->stream), "histogram walk");
     BT_CUDA(b, cudaStreamSynchronize(b->stream), "histogram walk");
-    b->launches += 1;
+    b->launches += 2;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, b->ev0, b->ev1);
     b->hist_ms = ms;

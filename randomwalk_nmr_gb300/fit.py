@@ -25,9 +25,10 @@ def decrease_factor(rho, res=1.0, d0=2.5):
 
 
 def fit_rho_batch(batch, targets, n_walkers, n_echoes, steps_per_echo, t2b, rho_init, res=1.0, d0=2.5,
-                  bounds=(0.5, 100.0), iters=8, bc="noflux"):
+                  bounds=(0.5, 100.0), iters=8, bc="noflux", method="auto"):
     """Fits one relaxivity per image. targets [n_images][n_echoes+1] normalised echo trains;
-    n_walkers [n_images]; rho_init [n_images][16] starting candidates. Returns a dict with the best
+    n_walkers [n_images]; rho_init [n_images][16] starting candidates; method as for Batch.cpmg
+    (with histograms the walk happens once, in the first iteration). Returns a dict with the best
     relaxivity and misfit per image, the candidate history and the GPU seconds spent."""
     targets = np.asarray(targets, np.float64)
     rho = np.array(rho_init, np.float64, copy=True)
@@ -39,7 +40,8 @@ def fit_rho_batch(batch, targets, n_walkers, n_echoes, steps_per_echo, t2b, rho_
     history = []
     loss = None
     for it in range(iters + 1):
-        echo, decho = batch.cpmg(decrease_factor(rho, res, d0), n_echoes, steps_per_echo, derivatives=True, bc=bc)
+        echo, decho = batch.cpmg(decrease_factor(rho, res, d0), n_echoes, steps_per_echo, derivatives=True, bc=bc,
+                                 method=method)
         gpu_s += batch.last_kernel_ms * 1e-3
         M = echo / nw * bulk
         J = decho / nw * bulk * dfdrho
