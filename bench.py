@@ -647,7 +647,7 @@ def main():
                 "launches_per_walk": launches_per_walk, "peak_source": peak_kind,
                 "note": ("achieved = bit-block bytes gathered per walker-step (4 B per block word) x walker-steps / "
                          "walk-kernel time, against the measured HBM copy peak; the gathers are L2-served "
-                         "(ncu: 93% L2 hit, 33 MB DRAM per launch), so the binding roof is instruction issue, "
+                         "(ncu: 95.5% L2 hit, 32 MB DRAM per launch), so the binding roof is instruction issue, "
                          "reported under 'issue'")}
     if inst:
         ach_issue = (value / world) * inst

@@ -85,6 +85,8 @@ struct rwnmr_ctx
     int nx = 0, ny = 0, nz = 0, bcols = 0, brows = 0, bdepth = 0, n_phases = 1, words = 1;
     DevBuf<uint64_t> blocks;
     DevBuf<uint8_t> labels;
+    DevBuf<uint32_t> morton; // Morton copy of the image for the noflux walk (mi.words null: none)
+    MortonImage mi;
 
     int64_t n = 0;
     bool has_walkers = false;
@@ -135,6 +137,7 @@ struct rwnmr_ctx
         im.bcr = bcols * brows;
         im.bc = bc;
         im.shift = shift;
+        im.mi = mi;
         return im;
     }
     WalkState state()
@@ -247,6 +250,7 @@ void rwnmr_ctx_destroy(rwnmr_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto *b : {&c->blocks}) b->release();
     c->labels.release();
+    c->morton.release();
     c->x0.release(); c->y0.release(); c->z0.release();
     c->x.release(); c->y.release(); c->z.release();
     c->seed0.release(); c->seed.release(); c->coll.release();
@@ -296,6 +300,50 @@ static rwnmr_status set_dims(rwnmr_ctx *c, int32_t nx, int32_t ny, int32_t nz, i
     return RWNMR_OK;
 }
 
+// Builds the Morton copy of the uploaded image when the power-of-two box around it holds at most
+// four times its voxels and fits 32-bit indices; otherwise the walks use the bit-block layout.
+static rwnmr_status build_morton(rwnmr_ctx *c)
+{
+    c->mi = MortonImage{};
+    auto bits = [](int n) {
+        int b = 0;
+        while ((1ll << b) < n) b++;
+        return b;
+    };
+    const int bx = bits(c->nx), by = bits(c->ny), bz = bits(c->nz);
+    const int total = bx + by + bz;
+    if (total > 32) return RWNMR_OK;
+    const uint64_t padded = 1ull << total;
+    if (padded > 4ull * (uint64_t)c->nx * c->ny * c->nz) return RWNMR_OK;
+    MortonImage m;
+    int pos = 0;
+    for (int i = 0; i < std::max(bx, std::max(by, bz)); i++)
+    {
+        if (i < bx) m.mx |= 1u << pos++;
+        if (i < by) m.my |= 1u << pos++;
+        if (i < bz) m.mz |= 1u << pos++;
+    }
+    m.ex = dilate_bits((uint32_t)c->nx - 1, m.mx);
+    m.ey = dilate_bits((uint32_t)c->ny - 1, m.my);
+    m.ez = dilate_bits((uint32_t)c->nz - 1, m.mz);
+    const uint32_t n_words = (uint32_t)std::max<uint64_t>(1, padded >> 5);
+    if (c->morton.ensure((size_t)n_words * c->words) != cudaSuccess)
+    {
+        cudaGetLastError(); // no room for the copy: the walks use the bit-block layout
+        c->morton.release();
+        return RWNMR_OK;
+    }
+    m.words = c->morton.p;
+    DevImage im = c->image(RWNMR_BC_NOFLUX, 0);
+    im.mi = m;
+    RW_CUDA(c, launch_morton_build(im, c->words, n_words, c->morton.p, c->stream), "Morton image");
+    c->launches++;
+    c->mi = m;
+    return RWNMR_OK;
+}
+
+int32_t rwnmr_image_layout(const rwnmr_ctx *c) { return c && c->has_image && c->mi.words ? 1 : 0; }
+
 rwnmr_status rwnmr_image_upload_labels(rwnmr_ctx *c, const uint8_t *labels, int32_t nx, int32_t ny, int32_t nz,
                                        int32_t n_phases)
 {
@@ -315,6 +363,8 @@ rwnmr_status rwnmr_image_upload_labels(rwnmr_ctx *c, const uint8_t *labels, int3
     c->launches++;
     RW_TRY(c->check_status("image packing"));
     if (c->n_phases == 1) c->labels.release();
+    RW_TRY(build_morton(c));
+    RW_CUDA(c, cudaStreamSynchronize(c->stream), "Morton image");
     c->has_image = true;
     return RWNMR_OK;
 }
@@ -346,6 +396,7 @@ rwnmr_status rwnmr_image_upload(rwnmr_ctx *c, const uint64_t *blocks, int32_t nx
     const int64_t nb = (int64_t)c->bcols * c->brows * c->bdepth;
     RW_CUDA(c, c->blocks.ensure((size_t)nb), "image blocks");
     RW_CUDA(c, cudaMemcpyAsync(c->blocks.p, blocks, (size_t)nb * 8, cudaMemcpyHostToDevice, c->stream), "blocks upload");
+    RW_TRY(build_morton(c));
     RW_CUDA(c, cudaStreamSynchronize(c->stream), "blocks upload");
     c->has_image = true;
     return RWNMR_OK;

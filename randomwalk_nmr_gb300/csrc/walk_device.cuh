@@ -33,6 +33,20 @@ enum
 // reference's uint64 block array itself (little-endian halves); for W > 1 one aligned 8- or
 // 16-byte load returns the solid bit and the phase bits of a voxel. Blocks are indexed in 32 bits
 // (images of fewer than 2^31 blocks, checked on the host).
+// Morton (bit-interleaved) copy of the image for the noflux walk without voxel division. A voxel's
+// index P interleaves the bits of x, y and z (each axis padded to a power of two; masks mx, my, mz
+// give each axis' bit positions). Word w holds the solid bits of voxels P = 32w .. 32w + 31, followed
+// by W - 1 phase bit-planes, so a step's gather address is P >> 5 and its bit P & 31. A move along one
+// axis is an increment or decrement of that axis' bit field alone ("dilated" arithmetic:
+// ((P | ~m) + 1) & m steps the field up, ((P & m) - 1) & m down), and the noflux edge test compares
+// the field with the dilated coordinate of the last voxel (dilation preserves order).
+struct MortonImage
+{
+    const uint32_t *__restrict__ words = nullptr; // null: no Morton copy
+    uint32_t mx = 0, my = 0, mz = 0;              // bit masks of each axis in P
+    uint32_t ex = 0, ey = 0, ez = 0;              // dilated coordinate n - 1 along each axis
+};
+
 struct DevImage
 {
     const uint64_t *__restrict__ blocks;
@@ -41,7 +55,27 @@ struct DevImage
     int32_t bcr; // bcols * brows
     int32_t bc;  // runtime boundary condition (BC_GENERIC path)
     int32_t shift;
+    MortonImage mi;
 };
+
+// Scatters the low bits of v onto the set bits of mask (lowest first), and gathers them back.
+__host__ __device__ inline uint32_t dilate_bits(uint32_t v, uint32_t mask)
+{
+    uint32_t r = 0;
+    for (uint32_t m = mask; m; m &= m - 1)
+    {
+        if (v & 1u) r |= m & (~m + 1u);
+        v >>= 1;
+    }
+    return r;
+}
+__host__ __device__ inline uint32_t undilate_bits(uint32_t p, uint32_t mask)
+{
+    uint32_t r = 0, bit = 1;
+    for (uint32_t m = mask; m; m &= m - 1, bit <<= 1)
+        if (p & m & (~m + 1u)) r |= bit;
+    return r;
+}
 
 // 64-bit words per bit-block for NP phase slots (1, 2 or 4).
 template <int NP>
@@ -316,6 +350,58 @@ __device__ __forceinline__ void walker_step(const DevImage &im, WalkerPos &p, ui
             p.oz = coz;
         }
     }
+}
+
+// Per direction r (0:N(-y) 1:W(-x) 2:S(+y) 3:E(+x) 4:Up(+z) 5:Down(-z)) of the Morton walk: the moving
+// axis' bit mask m, the field value at which the move is reversed (the last voxel for a move up, 0 for
+// a move down), and the steps to subtract from the axis field f = P & m for the move and for its
+// reversal: in dilated arithmetic (f - m) & m is f + 1 and (f - 1) & m is f - 1. Kept in shared
+// memory, so that decoding a direction is one lookup instead of integer compares and selects.
+__host__ __device__ inline uint4 morton_direction(const MortonImage &mi, int r)
+{
+    const uint32_t m = r >= 4 ? mi.mz : ((r & 1) ? mi.mx : mi.my);
+    const bool up = r == 2 || r == 3 || r == 4;
+    const uint32_t edge = up ? (r >= 4 ? mi.ez : ((r & 1) ? mi.ex : mi.ey)) : 0u;
+    return make_uint4(m, edge, up ? m : 1u, up ? 1u : m);
+}
+
+// One noflux step on the Morton copy (see MortonImage): the same xorshift64 draw, direction and
+// reversal rule as walker_step<BC_NOFLUX>, with the position held as the Morton index P. dirs: the
+// six morton_direction entries.
+template <int W>
+__device__ __forceinline__ void morton_step(const MortonImage &mi, const uint4 *dirs, uint32_t &P, uint64_t &seed,
+                                            bool &wall, int &phase)
+{
+    seed = xorshift64(seed);
+    const uint4 d = dirs[mod6(seed)];
+    const uint32_t f = P & d.x;
+    // a move off the image is reversed (walker.h:444-491): a move up at the last voxel goes down, a
+    // move down at voxel 0 goes up (every axis has at least two voxels)
+    const uint32_t step = f == d.y ? d.w : d.z;
+    const uint32_t Pn = ((f - step) & d.x) | (P & ~d.x);
+    const uint32_t *wp = mi.words + (size_t)(Pn >> 5) * W;
+    // bit Pn & 31 of each word: funnel shifts use the low five bits of the shift
+    uint32_t solid;
+    phase = 0;
+    if (W == 1)
+    {
+        solid = __ldg(wp);
+    }
+    else if (W == 2)
+    {
+        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(wp));
+        solid = v.x;
+        phase = (int)(__funnelshift_r(v.y, v.y, Pn) & 1u);
+    }
+    else
+    {
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(wp));
+        solid = v.x;
+        phase = (int)((__funnelshift_r(v.y, v.y, Pn) & 1u) | ((__funnelshift_r(v.z, v.z, Pn) & 1u) << 1) |
+                      ((__funnelshift_r(v.w, v.w, Pn) & 1u) << 2));
+    }
+    wall = (__funnelshift_r(solid, solid, Pn) & 1u) != 0;
+    if (!wall) P = Pn;
 }
 
 // Fixed-point energy (scale 2^63) of a walker with per-phase collision counts c[]: the product of

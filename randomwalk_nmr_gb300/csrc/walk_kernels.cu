@@ -64,17 +64,22 @@ constexpr int cpmg_min_blocks()
 
 // SPE: steps per echo known at compile time (1, 2 or 3, the common cases; 0 = read from the launch),
 // so the step loop unrolls away.
-template <int BC, int NP, bool PACK, bool WF, int SPE>
+// MORTON (noflux, no voxel division): the walk runs on the image's Morton copy with the position held
+// as one Morton index (morton_step), converted from and back to x, y, z once per launch.
+template <int BC, int NP, bool PACK, bool WF, int SPE, bool MORTON = false>
 __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, WF>()))
     cpmg_walk_kernel(DevImage im, WalkState st, CpmgLaunch L)
 {
     static_assert(!PACK || NP == 2, "packed collision counts are for two phases");
     static_assert(!WF || NP == 1, "per-walker decrease factors are for single-phase images");
+    static_assert(!MORTON || BC == BC_NOFLUX, "the Morton walk is the noflux walk");
     constexpr int W = WordsPerBlock<NP>::value;
     constexpr int NG = PACK ? 1 : NP; // collision-count words per echo
     constexpr int KK = 3 + NG;        // values kept per echo
     constexpr int K = 3 + NP;         // values per echo in the accumulators
     __shared__ unsigned long long sacc[32 * K];
+    __shared__ uint4 sdir[6]; // MORTON: direction table
+    if (MORTON && threadIdx.x < 6) sdir[threadIdx.x] = morton_direction(im.mi, threadIdx.x);
 
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -107,6 +112,9 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
         }
         init_image_coords<BC>(im, p);
     }
+    uint32_t P = 0; // MORTON: Morton index of the position
+    if (MORTON && active)
+        P = dilate_bits((uint32_t)p.x, im.mi.mx) | dilate_bits((uint32_t)p.y, im.mi.my) | dilate_bits((uint32_t)p.z, im.mi.mz);
 
     double fw = 1.0, ew = 1.0; // WF: decrease factor and energy of this walker
     if (WF && active)
@@ -153,7 +161,10 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                 {
                     bool wall;
                     int ph;
-                    walker_step<BC, W>(im, p, seed, wall, ph);
+                    if (MORTON)
+                        morton_step<W>(im.mi, sdir, P, seed, wall, ph);
+                    else
+                        walker_step<BC, W>(im, p, seed, wall, ph);
                     if (PACK) g[0] += (wall ? 1u : 0u) << (ph << 4);
                     else
                     {
@@ -236,6 +247,12 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
 
     if (active)
     {
+        if (MORTON)
+        {
+            p.x = (int)undilate_bits(P, im.mi.mx);
+            p.y = (int)undilate_bits(P, im.mi.my);
+            p.z = (int)undilate_bits(P, im.mi.mz);
+        }
         st.x[i] = p.x;
         st.y[i] = p.y;
         st.z[i] = p.z;
@@ -582,6 +599,35 @@ __global__ void pack_blocks_kernel(const uint8_t *__restrict__ labels, int nx, i
 }
 
 // ---------------------------------------------------------------------------------------------
+// Morton copy of an image (see MortonImage): one thread per Morton word gathers its 32 voxels' solid
+// and phase bits from the bit-block layout; voxels of the padding beyond the image stay 0 (no walker
+// reaches them: noflux walks stay inside).
+__global__ void morton_build_kernel(DevImage im, int W, uint32_t n_words, uint32_t *__restrict__ out)
+{
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= n_words) return;
+    uint32_t acc[4] = {0, 0, 0, 0};
+    const uint32_t *base = reinterpret_cast<const uint32_t *>(im.blocks);
+    for (uint32_t b = 0; b < 32; b++)
+    {
+        const uint32_t P = (w << 5) | b;
+        const uint32_t x = undilate_bits(P, im.mi.mx), y = undilate_bits(P, im.mi.my), z = undilate_bits(P, im.mi.mz);
+        if (x >= (uint32_t)im.nx || y >= (uint32_t)im.ny || z >= (uint32_t)im.nz) continue;
+        const uint32_t blk = (x >> 2) + (y >> 2) * (uint32_t)im.bcols + (z >> 2) * (uint32_t)im.bcr;
+        const uint32_t bit = (x & 3) | ((y & 3) << 2) | ((z & 3) << 4);
+        const uint32_t *bp = base + (size_t)blk * (2 * W) + (bit >> 5) * W;
+        for (int k = 0; k < W; k++) acc[k] |= ((bp[k] >> (bit & 31)) & 1u) << b;
+    }
+    for (int k = 0; k < W; k++) out[(size_t)w * W + k] = acc[k];
+}
+
+cudaError_t launch_morton_build(const DevImage &im, int W, uint32_t n_words, uint32_t *out, cudaStream_t s)
+{
+    morton_build_kernel<<<(n_words + 255) / 256, 256, 0, s>>>(im, W, n_words, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
 // Host-side dispatch over the (boundary condition, phase count) template grid.
 namespace
 {
@@ -607,19 +653,31 @@ cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkS
             constexpr int BC = decltype(bcc)::value;
             // packed counts: a lane's half-word holds at most steps_per_echo < 2^16 collisions, and a
             // recorded echo's warp sum of a half at most 32 * steps_per_echo < 2^16
-            auto run = [&](auto spe) {
+            auto run_m = [&](auto spe, auto mort) {
                 constexpr int SPE = decltype(spe)::value;
+                constexpr bool M = decltype(mort)::value;
                 if constexpr (NP == 1)
                 {
                     if (L.wf)
-                        cpmg_walk_kernel<BC, 1, false, true, SPE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                        cpmg_walk_kernel<BC, 1, false, true, SPE, M><<<grid, kWalkThreads, 0, s>>>(im, st, L);
                     else
-                        cpmg_walk_kernel<BC, 1, false, false, SPE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                        cpmg_walk_kernel<BC, 1, false, false, SPE, M><<<grid, kWalkThreads, 0, s>>>(im, st, L);
                 }
                 else if (NP == 2 && L.steps_per_echo <= (L.record ? 2047 : 65535))
-                    cpmg_walk_kernel<BC, NP, NP == 2, false, SPE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    cpmg_walk_kernel<BC, NP, NP == 2, false, SPE, M><<<grid, kWalkThreads, 0, s>>>(im, st, L);
                 else
-                    cpmg_walk_kernel<BC, NP, false, false, SPE><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    cpmg_walk_kernel<BC, NP, false, false, SPE, M><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            };
+            auto run = [&](auto spe) {
+                if constexpr (BC == BC_NOFLUX)
+                {
+                    if (im.mi.words)
+                    {
+                        run_m(spe, std::true_type{});
+                        return;
+                    }
+                }
+                run_m(spe, std::false_type{});
             };
             const int spe = L.record ? L.steps_per_echo : 0;
             if (spe == 1) run(std::integral_constant<int, 1>{});

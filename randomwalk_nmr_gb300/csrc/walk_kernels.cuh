@@ -124,6 +124,8 @@ cudaError_t launch_pfgse_walk(int bc_key, int np, const DevImage &im, const Walk
                               dim3 grid, cudaStream_t s);
 cudaError_t launch_pfgse_phase(const PhaseLaunch &L, int n_delta, int n_g, cudaStream_t s);
 cudaError_t launch_pfgse_direct(const DirectLaunch &L, int n_delta, int blocks, cudaStream_t s);
+// Builds the Morton copy im.mi describes (n_words x W uint32) from im's bit-blocks.
+cudaError_t launch_morton_build(const DevImage &im, int W, uint32_t n_words, uint32_t *out, cudaStream_t s);
 cudaError_t launch_pack_blocks(const uint8_t *labels, int nx, int ny, int nz, int bcols, int brows, int64_t nblocks,
                                int words, uint64_t *out, unsigned *status, cudaStream_t s);
 
