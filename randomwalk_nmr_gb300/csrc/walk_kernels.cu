@@ -363,11 +363,17 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_adjoint_kernel(DevImage im,
 //   * for any other gradient direction, each walker's displacement and FP64 energy, measured by
 //     pfgse_direct_kernel.
 // WF: per-walker decrease factors, energies as FP64 repeated products (see cpmg_walk_kernel).
-template <int BC, int NP, bool WF>
+// MORTON (noflux, no voxel division): steps on the image's Morton copy (see cpmg_walk_kernel); the
+// position is converted back to x, y, z at each exposure time.
+template <int BC, int NP, bool WF, bool MORTON = false>
 __global__ void __launch_bounds__(kWalkThreads) pfgse_walk_kernel(DevImage im, WalkState st, PfgseLaunch L)
 {
     static_assert(!WF || NP == 1, "per-walker decrease factors are for single-phase images");
+    static_assert(!MORTON || BC == BC_NOFLUX, "the Morton walk is the noflux walk");
     constexpr int W = WordsPerBlock<NP>::value;
+    __shared__ uint4 sdir[6]; // MORTON: direction table
+    if (MORTON && threadIdx.x < 6) sdir[threadIdx.x] = morton_direction(im.mi, threadIdx.x);
+    if (MORTON) __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     bool active = i < st.n;
@@ -396,6 +402,9 @@ __global__ void __launch_bounds__(kWalkThreads) pfgse_walk_kernel(DevImage im, W
     const double fw = (WF && active) ? L.wf[i] : 1.0;
     double ew = 1.0;
     uint32_t c_done = 0; // WF: collisions already folded into ew
+    uint32_t P = 0;      // MORTON: Morton index of the position
+    if (MORTON && active)
+        P = dilate_bits((uint32_t)p.x, im.mi.mx) | dilate_bits((uint32_t)p.y, im.mi.my) | dilate_bits((uint32_t)p.z, im.mi.mz);
     int done = 0;
     for (int d = 0; d < L.n_delta; d++)
     {
@@ -407,9 +416,18 @@ __global__ void __launch_bounds__(kWalkThreads) pfgse_walk_kernel(DevImage im, W
             {
                 bool wall;
                 int ph;
-                walker_step<BC, W>(im, p, seed, wall, ph);
+                if (MORTON)
+                    morton_step<W>(im.mi, sdir, P, seed, wall, ph);
+                else
+                    walker_step<BC, W>(im, p, seed, wall, ph);
 #pragma unroll
                 for (int q = 0; q < NP; q++) c[q] += (wall && ph == q) ? 1u : 0u;
+            }
+            if (MORTON)
+            {
+                p.x = (int)undilate_bits(P, im.mi.mx);
+                p.y = (int)undilate_bits(P, im.mi.my);
+                p.z = (int)undilate_bits(P, im.mi.mz);
             }
         }
         if (WF)
@@ -715,15 +733,27 @@ cudaError_t launch_pfgse_walk(int bc_key, int np, const DevImage &im, const Walk
         constexpr int NP = decltype(npc)::value;
         with_bc<NP>(bc_key, [&](auto bcc) {
             constexpr int BC = decltype(bcc)::value;
-            if constexpr (NP == 1)
-            {
-                if (L.wf)
-                    pfgse_walk_kernel<BC, 1, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            auto run = [&](auto mort) {
+                constexpr bool M = decltype(mort)::value;
+                if constexpr (NP == 1)
+                {
+                    if (L.wf)
+                        pfgse_walk_kernel<BC, 1, true, M><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    else
+                        pfgse_walk_kernel<BC, 1, false, M><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                }
                 else
-                    pfgse_walk_kernel<BC, 1, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    pfgse_walk_kernel<BC, NP, false, M><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            };
+            if constexpr (BC == BC_NOFLUX)
+            {
+                if (im.mi.words)
+                {
+                    run(std::true_type{});
+                    return;
+                }
             }
-            else
-                pfgse_walk_kernel<BC, NP, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            run(std::false_type{});
         });
     };
     if (np == 1) go(std::integral_constant<int, 1>{});
