@@ -270,11 +270,16 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
 // walker replays its trajectory from its stored seed and accumulates sum_e g[e] dE(e)/df_q in FP64
 // (a few multiply-adds per walker-echo, no cross-lane FP64), then reduces once at the end.
 // partial: [gridDim.x][NP], summed on the host in block order (deterministic).
-template <int BC, int NP>
+// MORTON (noflux, no voxel division): the replay steps on the image's Morton copy.
+template <int BC, int NP, bool MORTON = false>
 __global__ void __launch_bounds__(kWalkThreads) cpmg_adjoint_kernel(DevImage im, WalkState st, AdjointLaunch L)
 {
+    static_assert(!MORTON || BC == BC_NOFLUX, "the Morton walk is the noflux walk");
     constexpr int W = WordsPerBlock<NP>::value;
     __shared__ double sred[kWalkThreads / 32][NP];
+    __shared__ uint4 sdir[6]; // MORTON: direction table
+    if (MORTON && threadIdx.x < 6) sdir[threadIdx.x] = morton_direction(im.mi, threadIdx.x);
+    if (MORTON) __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     bool active = i < st.n;
@@ -301,6 +306,9 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_adjoint_kernel(DevImage im,
         }
         init_image_coords<BC>(im, p);
     }
+    uint32_t P = 0; // MORTON: Morton index of the position
+    if (MORTON && active)
+        P = dilate_bits((uint32_t)p.x, im.mi.mx) | dilate_bits((uint32_t)p.y, im.mi.my) | dilate_bits((uint32_t)p.z, im.mi.mz);
     if (active)
     {
         const double *T = L.t;
@@ -311,7 +319,10 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_adjoint_kernel(DevImage im,
             {
                 bool wall;
                 int ph;
-                walker_step<BC, W>(im, p, seed, wall, ph);
+                if (MORTON)
+                    morton_step<W>(im.mi, sdir, P, seed, wall, ph);
+                else
+                    walker_step<BC, W>(im, p, seed, wall, ph);
 #pragma unroll
                 for (int q = 0; q < NP; q++) c[q] += (wall && ph == q) ? 1u : 0u;
             }
@@ -717,7 +728,15 @@ cudaError_t launch_cpmg_adjoint(int bc_key, int np, const DevImage &im, const Wa
         constexpr int NP = decltype(npc)::value;
         with_bc<NP>(bc_key, [&](auto bcc) {
             constexpr int BC = decltype(bcc)::value;
-            cpmg_adjoint_kernel<BC, NP><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+            if constexpr (BC == BC_NOFLUX)
+            {
+                if (im.mi.words)
+                {
+                    cpmg_adjoint_kernel<BC, NP, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    return;
+                }
+            }
+            cpmg_adjoint_kernel<BC, NP, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
         });
     };
     if (np == 1) go(std::integral_constant<int, 1>{});
