@@ -150,12 +150,17 @@ def cpu_baseline(labels, n_phases, walkers, spe, echoes, f, bc, target_s=15.0):
     o = Oracle()
     threads = os.cpu_count() or 1
     x, y, z, s = walkers
-    # calibrate on a small sample, then size the timed sample to ~target_s
+    # calibrate on a small sample, then size the timed sample to ~target_s; a one-echo call measures
+    # the per-call fixed cost (image packing), which the rate must not include
     n0 = min(len(x), 256 * threads)
     e0 = min(echoes, 2000)
+    small = (x[:n0], y[:n0], z[:n0], s[:n0])
     t0 = time.perf_counter()
-    o.cpmg(labels, (x[:n0], y[:n0], z[:n0], s[:n0]), e0, spe, f, bc=bc, n_phases=n_phases, threads=threads)
-    rate = n0 * e0 * spe / (time.perf_counter() - t0)
+    o.cpmg(labels, small, 1, spe, f, bc=bc, n_phases=n_phases, threads=threads)
+    fixed = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    o.cpmg(labels, small, e0, spe, f, bc=bc, n_phases=n_phases, threads=threads)
+    rate = n0 * e0 * spe / max(time.perf_counter() - t0 - fixed, 1e-3)
     n = int(max(threads * 4, min(len(x), rate * target_s / (echoes * spe))))
     sample = (x[:n], y[:n], z[:n], s[:n])
     t0 = time.perf_counter()

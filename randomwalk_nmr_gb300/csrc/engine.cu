@@ -744,6 +744,10 @@ rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const 
     L.grad = c->grad.p;
     L.partial = c->partial.p;
     L.status = c->status.p;
+    // with every f_q > 0, dE/df_q = (c_q / f_q) E: the kernel sums g E c_q and the host divides
+    L.scaled = 1;
+    for (int q = 0; q < c->n_phases; q++)
+        if (!(p->dfactor[q] > 0.0)) L.scaled = 0;
     RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
     if (c->n > 0)
     {
@@ -764,7 +768,7 @@ rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const 
     {
         double s = 0.0;
         for (unsigned b = 0; b < grid.x; b++) s += part[(size_t)b * slots + q];
-        grad_dfactor[q] = s;
+        grad_dfactor[q] = L.scaled ? s / p->dfactor[q] : s;
     }
     // echo 0 does not depend on the decrease factors
     return RWNMR_OK;

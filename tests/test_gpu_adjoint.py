@@ -65,3 +65,21 @@ def test_adjoint_zero_gradient_is_zero(engine):
     setup(engine, 1)
     adj = engine.cpmg_adjoint(20, 1, dfactor(10.0), np.zeros(21))
     assert np.all(adj == 0.0)
+
+
+@pytest.mark.parametrize("f", [[0.0, 0.97], [0.55, 0.0, 0.9, 0.999]])
+def test_adjoint_with_a_zero_decrease_factor(engine, oracle, f):
+    """With every f_q > 0 the kernel sums g E c_q and divides by f_q; a zero factor takes the
+    direct derivative (c_q f_q^(c_q - 1) is 1 at c_q = 1 while E is 0). Both against the pathwise
+    gradient."""
+    n_phases = len(f)
+    lab, w = setup(engine, n_phases, seed=5, n=1500)
+    n_echoes, spe = 25, 2
+    rng = np.random.default_rng(2)
+    grad = rng.normal(size=n_echoes + 1)
+    ref = pathwise_gradient(oracle, lab, w, n_echoes, spe, f, grad, n_phases)
+    adj = engine.cpmg_adjoint(n_echoes, spe, np.array(f), grad)
+    np.testing.assert_allclose(adj, ref, rtol=1e-10, atol=1e-12 * np.max(np.abs(ref)))
+    g2 = engine.cpmg_adjoint(n_echoes, spe, np.array([v if v > 0 else 0.5 for v in f]), grad)
+    ref2 = pathwise_gradient(oracle, lab, w, n_echoes, spe, [v if v > 0 else 0.5 for v in f], grad, n_phases)
+    np.testing.assert_allclose(g2, ref2, rtol=1e-10, atol=1e-12 * np.max(np.abs(ref2)))
