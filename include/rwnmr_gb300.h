@@ -82,7 +82,9 @@ int32_t rwnmr_image_layout(const rwnmr_ctx *ctx);
 
 /* ---- walkers --------------------------------------------------------------------------- */
 /* Initial state (Walker::initialPosition / initialSeed). Positions are in walk units (voxels
- * << voxel-division shift). */
+ * << voxel-division shift). The engine stores the walkers sorted by a coarse Morton key of their
+ * start voxel (a stable sort on the GPU), so that neighbouring threads walk neighbouring walkers;
+ * every per-walker input and output of this API is in the upload order. */
 rwnmr_status rwnmr_walkers_upload(rwnmr_ctx *ctx, int64_t n, const int32_t *x0, const int32_t *y0, const int32_t *z0,
                                   const uint64_t *seed0);
 /* State after the last run: positions, current RNG state, per-phase collision totals

@@ -90,6 +90,12 @@ struct rwnmr_ctx
 
     int64_t n = 0;
     bool has_walkers = false;
+    // walkers are stored in spatial order: perm[k] = upload index of the walker at k (host copy
+    // fetched when a per-walker input or output needs it)
+    DevBuf<int32_t> perm;
+    DevBuf<uint32_t> order_scratch;
+    std::vector<int32_t> h_perm;
+    bool h_perm_valid = false;
     bool has_wf = false; // per-walker decrease factors uploaded
     DevBuf<double> wf, wenergy;
     DevBuf<int32_t> x0, y0, z0, x, y, z;
@@ -195,6 +201,22 @@ rwnmr_status check_walker_dfactor(rwnmr_ctx *ctx)
     return RWNMR_OK;
 }
 
+// Host copy of the walker order (upload index of each stored walker).
+rwnmr_status host_perm(rwnmr_ctx *c)
+{
+    if (c->h_perm_valid) return RWNMR_OK;
+    c->h_perm.resize((size_t)c->n);
+    if (c->n > 0)
+    {
+        rwnmr_status r = c->cuda(cudaMemcpyAsync(c->h_perm.data(), c->perm.p, (size_t)c->n * 4, cudaMemcpyDeviceToHost,
+                                                 c->stream), "walker order");
+        if (r == RWNMR_OK) r = c->cuda(cudaStreamSynchronize(c->stream), "walker order");
+        if (r != RWNMR_OK) return r;
+    }
+    c->h_perm_valid = true;
+    return RWNMR_OK;
+}
+
 rwnmr_status check_dfactor(rwnmr_ctx *ctx, const double *f)
 {
     if (!f) return ctx->fail(RWNMR_ERR_INVALID, "dfactor is NULL");
@@ -251,6 +273,7 @@ void rwnmr_ctx_destroy(rwnmr_ctx *c)
     for (auto *b : {&c->blocks}) b->release();
     c->labels.release();
     c->morton.release();
+    c->perm.release(); c->order_scratch.release();
     c->x0.release(); c->y0.release(); c->z0.release();
     c->x.release(); c->y.release(); c->z.release();
     c->seed0.release(); c->seed.release(); c->coll.release();
@@ -441,13 +464,24 @@ rwnmr_status rwnmr_walkers_upload(rwnmr_ctx *c, int64_t n, const int32_t *x0, co
     RW_CUDA(c, c->x.ensure(m), "walkers"); RW_CUDA(c, c->y.ensure(m), "walkers"); RW_CUDA(c, c->z.ensure(m), "walkers");
     RW_CUDA(c, c->seed0.ensure(m), "walkers"); RW_CUDA(c, c->seed.ensure(m), "walkers");
     RW_CUDA(c, c->coll.ensure(m * 4), "walkers");
+    RW_CUDA(c, c->perm.ensure(m), "walker order");
+    RW_CUDA(c, c->order_scratch.ensure(walker_order_scratch_words((int64_t)m)), "walker order");
+    c->h_perm_valid = false;
     if (n > 0)
     {
         const size_t b4 = (size_t)n * 4, b8 = (size_t)n * 8;
-        RW_CUDA(c, cudaMemcpyAsync(c->x0.p, x0, b4, cudaMemcpyHostToDevice, c->stream), "walkers upload");
-        RW_CUDA(c, cudaMemcpyAsync(c->y0.p, y0, b4, cudaMemcpyHostToDevice, c->stream), "walkers upload");
-        RW_CUDA(c, cudaMemcpyAsync(c->z0.p, z0, b4, cudaMemcpyHostToDevice, c->stream), "walkers upload");
-        RW_CUDA(c, cudaMemcpyAsync(c->seed0.p, seed0, b8, cudaMemcpyHostToDevice, c->stream), "walkers upload");
+        // stage in upload order, sort by start voxel, gather into the stored order
+        RW_CUDA(c, cudaMemcpyAsync(c->x.p, x0, b4, cudaMemcpyHostToDevice, c->stream), "walkers upload");
+        RW_CUDA(c, cudaMemcpyAsync(c->y.p, y0, b4, cudaMemcpyHostToDevice, c->stream), "walkers upload");
+        RW_CUDA(c, cudaMemcpyAsync(c->z.p, z0, b4, cudaMemcpyHostToDevice, c->stream), "walkers upload");
+        RW_CUDA(c, cudaMemcpyAsync(c->seed.p, seed0, b8, cudaMemcpyHostToDevice, c->stream), "walkers upload");
+        int shift = 0; // keep 10 bits per axis of the image's coordinates
+        if (c->has_image)
+            while ((std::max(c->nx, std::max(c->ny, c->nz)) - 1) >> (10 + shift)) shift++;
+        RW_CUDA(c, walker_order(c->x.p, c->y.p, c->z.p, n, shift, c->order_scratch.p, c->perm.p, c->stream), "walker order");
+        RW_CUDA(c, gather_walkers(c->perm.p, n, c->x.p, c->y.p, c->z.p, c->seed.p, c->x0.p, c->y0.p, c->z0.p,
+                                  c->seed0.p, c->stream), "walker order");
+        c->launches += 8;
         RW_CUDA(c, cudaMemcpyAsync(c->x.p, c->x0.p, b4, cudaMemcpyDeviceToDevice, c->stream), "walkers init");
         RW_CUDA(c, cudaMemcpyAsync(c->y.p, c->y0.p, b4, cudaMemcpyDeviceToDevice, c->stream), "walkers init");
         RW_CUDA(c, cudaMemcpyAsync(c->z.p, c->z0.p, b4, cudaMemcpyDeviceToDevice, c->stream), "walkers init");
@@ -466,22 +500,34 @@ rwnmr_status rwnmr_walkers_download(rwnmr_ctx *c, int32_t *x, int32_t *y, int32_
     if (!c->has_walkers) return c->fail(RWNMR_ERR_STATE, "no walkers uploaded");
     const int64_t n = c->n;
     if (n == 0) return RWNMR_OK;
+    RW_TRY(host_perm(c));
+    const std::vector<int32_t> &pm = c->h_perm;
     const size_t b4 = (size_t)n * 4;
-    if (x) RW_CUDA(c, cudaMemcpyAsync(x, c->x.p, b4, cudaMemcpyDeviceToHost, c->stream), "walkers download");
-    if (y) RW_CUDA(c, cudaMemcpyAsync(y, c->y.p, b4, cudaMemcpyDeviceToHost, c->stream), "walkers download");
-    if (z) RW_CUDA(c, cudaMemcpyAsync(z, c->z.p, b4, cudaMemcpyDeviceToHost, c->stream), "walkers download");
-    if (seed) RW_CUDA(c, cudaMemcpyAsync(seed, c->seed.p, b4 * 2, cudaMemcpyDeviceToHost, c->stream), "walkers download");
+    std::vector<int32_t> tx(x ? n : 0), ty(y ? n : 0), tz(z ? n : 0);
+    std::vector<uint64_t> ts(seed ? n : 0);
     std::vector<uint32_t> tmp;
     const int P = c->n_phases;
+    if (x) RW_CUDA(c, cudaMemcpyAsync(tx.data(), c->x.p, b4, cudaMemcpyDeviceToHost, c->stream), "walkers download");
+    if (y) RW_CUDA(c, cudaMemcpyAsync(ty.data(), c->y.p, b4, cudaMemcpyDeviceToHost, c->stream), "walkers download");
+    if (z) RW_CUDA(c, cudaMemcpyAsync(tz.data(), c->z.p, b4, cudaMemcpyDeviceToHost, c->stream), "walkers download");
+    if (seed) RW_CUDA(c, cudaMemcpyAsync(ts.data(), c->seed.p, b4 * 2, cudaMemcpyDeviceToHost, c->stream), "walkers download");
     if (coll)
     {
         tmp.resize((size_t)n * P);
         RW_CUDA(c, cudaMemcpyAsync(tmp.data(), c->coll.p, b4 * P, cudaMemcpyDeviceToHost, c->stream), "walkers download");
     }
     RW_CUDA(c, cudaStreamSynchronize(c->stream), "walkers download");
-    if (coll)
-        for (int64_t i = 0; i < n; i++)
-            for (int q = 0; q < P; q++) coll[(size_t)i * P + q] = tmp[(size_t)q * n + i];
+    // back to upload order
+    for (int64_t k = 0; k < n; k++)
+    {
+        const size_t u = (size_t)pm[(size_t)k];
+        if (x) x[u] = tx[(size_t)k];
+        if (y) y[u] = ty[(size_t)k];
+        if (z) z[u] = tz[(size_t)k];
+        if (seed) seed[u] = ts[(size_t)k];
+        if (coll)
+            for (int q = 0; q < P; q++) coll[u * P + q] = tmp[(size_t)q * n + k];
+    }
     return RWNMR_OK;
 }
 
@@ -495,8 +541,11 @@ rwnmr_status rwnmr_walkers_set_dfactor(rwnmr_ctx *c, const double *dfactor)
             return c->fail(RWNMR_ERR_UNSUPPORTED, "decrease factor %g of walker %lld outside [0, 1]", dfactor[i], (long long)i);
     cudaSetDevice(c->device);
     RW_CUDA(c, c->wf.ensure((size_t)std::max<int64_t>(c->n, 1)), "walker decrease factors");
+    RW_TRY(host_perm(c));
+    std::vector<double> stored((size_t)c->n); // in the stored walker order
+    for (int64_t k = 0; k < c->n; k++) stored[(size_t)k] = dfactor[c->h_perm[(size_t)k]];
     if (c->n > 0)
-        RW_CUDA(c, cudaMemcpyAsync(c->wf.p, dfactor, (size_t)c->n * 8, cudaMemcpyHostToDevice, c->stream),
+        RW_CUDA(c, cudaMemcpyAsync(c->wf.p, stored.data(), (size_t)c->n * 8, cudaMemcpyHostToDevice, c->stream),
                 "walker decrease factors");
     RW_CUDA(c, cudaStreamSynchronize(c->stream), "walker decrease factors");
     c->has_wf = true;
@@ -684,10 +733,19 @@ rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p
     RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
     std::vector<unsigned long long> acc((size_t)(p->n_echoes + 1) * K);
     RW_CUDA(c, cudaMemcpyAsync(acc.data(), c->acc.p, acc.size() * 8, cudaMemcpyDeviceToHost, c->stream), "echo readback");
+    std::vector<double> ph;
     if (phase_out && c->n > 0)
-        RW_CUDA(c, cudaMemcpyAsync(phase_out, c->phase.p, (size_t)c->n * 8, cudaMemcpyDeviceToHost, c->stream),
+    {
+        ph.resize((size_t)c->n);
+        RW_CUDA(c, cudaMemcpyAsync(ph.data(), c->phase.p, (size_t)c->n * 8, cudaMemcpyDeviceToHost, c->stream),
                 "phase readback");
+    }
     RW_TRY(c->check_status("field cpmg walk"));
+    if (!ph.empty())
+    {
+        RW_TRY(host_perm(c));
+        for (int64_t k = 0; k < c->n; k++) phase_out[c->h_perm[(size_t)k]] = ph[(size_t)k];
+    }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->last_ms = ms;
@@ -837,11 +895,12 @@ static rwnmr_status map_impl(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t st
         std::vector<uint32_t> tmp((size_t)c->n * P);
         RW_CUDA(c, cudaMemcpyAsync(tmp.data(), c->coll.p, tmp.size() * 4, cudaMemcpyDeviceToHost, c->stream), "readback");
         RW_CUDA(c, cudaStreamSynchronize(c->stream), "readback");
+        RW_TRY(host_perm(c));
         for (int64_t i = 0; i < c->n; i++)
         {
             uint32_t s = 0;
             for (int q = 0; q < P; q++) s += tmp[(size_t)q * c->n + i];
-            collisions[i] = s;
+            collisions[c->h_perm[(size_t)i]] = s;
         }
     }
     return RWNMR_OK;

@@ -125,6 +125,14 @@ cudaError_t launch_pfgse_walk(int bc_key, int np, const DevImage &im, const Walk
                               dim3 grid, cudaStream_t s);
 cudaError_t launch_pfgse_phase(const PhaseLaunch &L, int n_delta, int n_g, cudaStream_t s);
 cudaError_t launch_pfgse_direct(const DirectLaunch &L, int n_delta, int blocks, cudaStream_t s);
+// Spatial walker order (walker_order.cu): perm[k] = upload index of the walker stored at k, sorted
+// stably by a coarse Morton key of (x, y, z) >> shift. scratch: walker_order_scratch_words(n) uint32.
+size_t walker_order_scratch_words(int64_t n);
+cudaError_t walker_order(const int32_t *x, const int32_t *y, const int32_t *z, int64_t n, int shift, uint32_t *scratch,
+                         int32_t *perm, cudaStream_t s);
+// x0[k] = ux[perm[k]] (and y, z, seeds)
+cudaError_t gather_walkers(const int32_t *perm, int64_t n, const int32_t *ux, const int32_t *uy, const int32_t *uz,
+                           const uint64_t *us, int32_t *x0, int32_t *y0, int32_t *z0, uint64_t *s0, cudaStream_t s);
 // Builds the Morton copy im.mi describes (n_words x W uint32) from im's bit-blocks.
 cudaError_t launch_morton_build(const DevImage &im, int W, uint32_t n_words, uint32_t *out, cudaStream_t s);
 cudaError_t launch_pack_blocks(const uint8_t *labels, int nx, int ny, int nz, int bcols, int brows, int64_t nblocks,
