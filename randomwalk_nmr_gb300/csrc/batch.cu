@@ -51,6 +51,7 @@ struct BatchImage
     int64_t tab0;             // offset of this image's tables (u64 words)
     int64_t hist0;            // offset of this image's collision histogram (u32 words)
     int32_t u_shift;          // derivative scale exponent
+    MortonImage mi;           // Morton copy for the noflux histogram walk (words null: none)
 };
 
 struct WorkItem
@@ -263,6 +264,7 @@ template <int BC, int WPT>
 __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
 {
     __shared__ int s_item;
+    __shared__ uint4 sdir[6]; // Morton direction table of the current item's image
     for (;;)
     {
         if (threadIdx.x == 0) s_item = (int)atomicAdd(L.counter, 1u);
@@ -278,6 +280,18 @@ __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
         bool active[WPT];
         uint32_t c[WPT];
         load_walkers<BC, WPT>(L, w, im, p, seed, active, c);
+        // noflux images with a Morton copy take the Morton step (uniform over the CTA's item)
+        const bool mort = BC == BC_NOFLUX && img.mi.words != nullptr;
+        uint32_t P[WPT];
+        if (mort)
+        {
+            if (threadIdx.x < 6) sdir[threadIdx.x] = morton_direction(img.mi, threadIdx.x);
+#pragma unroll
+            for (int j = 0; j < WPT; j++)
+                P[j] = dilate_bits((uint32_t)p[j].x, img.mi.mx) | dilate_bits((uint32_t)p[j].y, img.mi.my) |
+                       dilate_bits((uint32_t)p[j].z, img.mi.mz);
+        }
+        __syncthreads();
         unsigned *H = L.hist + img.hist0;
         const int spe = L.steps_per_echo;
         for (int e = 0; e <= L.n_echoes; e++)
@@ -292,7 +306,10 @@ __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
                         {
                             bool wall;
                             int ph;
-                            walker_step<BC, 1>(im, p[j], seed[j], wall, ph);
+                            if (mort)
+                                morton_step<1>(img.mi, sdir, P[j], seed[j], wall, ph);
+                            else
+                                walker_step<BC, 1>(im, p[j], seed[j], wall, ph);
                             c[j] += wall ? 1u : 0u;
                         }
                     atomicAdd(H + row + c[j], 1u);
@@ -484,6 +501,7 @@ struct rwnmr_batch
     unsigned long long *d_tab = nullptr, *d_acc = nullptr;
     unsigned *d_counter = nullptr, *d_status = nullptr;
     double *d_f = nullptr;
+    uint32_t *d_morton = nullptr; // Morton copies of the images that have one
     size_t tab_words = 0, acc_words = 0;
     int n_items = 0, items_block = 0; // items_block: walkers per work item
     // pinned host staging and the captured graph
@@ -511,7 +529,7 @@ struct rwnmr_batch
         graph = nullptr;
         for (void *p : {(void *)d_blocks, (void *)d_images, (void *)d_items, (void *)d_x, (void *)d_y, (void *)d_z,
                         (void *)d_seed, (void *)d_tab, (void *)d_acc, (void *)d_counter,
-                        (void *)d_status, (void *)d_f})
+                        (void *)d_status, (void *)d_f, (void *)d_morton})
             if (p) cudaFree(p);
         d_blocks = nullptr;
         d_images = nullptr;
@@ -521,6 +539,7 @@ struct rwnmr_batch
         d_tab = d_acc = nullptr;
         d_counter = d_status = nullptr;
         d_f = nullptr;
+        d_morton = nullptr;
         if (d_hist) cudaFree(d_hist);
         if (d_hist_range) cudaFree(d_hist_range);
         d_hist = nullptr;
@@ -578,6 +597,42 @@ rwnmr_status upload(rwnmr_batch *b, int n_echoes, int spe)
         b->images[k].acc0 = (int64_t)k * (n_echoes + 1) * kCand * 4;
         b->images[k].hist0 = (int64_t)k * hist_words(n_echoes, spe);
         b->images[k].u_shift = us;
+    }
+    // Morton copies (single-phase: one word per 32 voxels) for the images whose box allows one
+    {
+        std::vector<uint32_t> words(ni, 0);
+        size_t total = 0;
+        for (int k = 0; k < ni; k++)
+        {
+            b->images[k].mi = morton_params(b->images[k].nx, b->images[k].ny, b->images[k].nz, words[k]);
+            total += words[k];
+        }
+        if (total)
+        {
+            // the block copies above ran on the default stream; the build reads them on b->stream
+            BT_CUDA(b, cudaStreamSynchronize(0), "batch image upload");
+            BT_CUDA(b, cudaMalloc(&b->d_morton, total * 4), "batch Morton images");
+            size_t mo = 0;
+            for (int k = 0; k < ni; k++)
+            {
+                if (!words[k]) continue;
+                BatchImage &bi = b->images[k];
+                bi.mi.words = b->d_morton + mo;
+                DevImage im{};
+                im.blocks = bi.blocks;
+                im.nx = bi.nx;
+                im.ny = bi.ny;
+                im.nz = bi.nz;
+                im.bcols = bi.bcols;
+                im.bcr = bi.bcr;
+                im.bc = RWNMR_BC_NOFLUX;
+                im.shift = 0;
+                im.mi = bi.mi;
+                BT_CUDA(b, launch_morton_build(im, 1, words[k], b->d_morton + mo, b->stream), "batch Morton images");
+                mo += words[k];
+            }
+            BT_CUDA(b, cudaStreamSynchronize(b->stream), "batch Morton images");
+        }
     }
     if (nw)
     {

@@ -328,28 +328,9 @@ static rwnmr_status set_dims(rwnmr_ctx *c, int32_t nx, int32_t ny, int32_t nz, i
 static rwnmr_status build_morton(rwnmr_ctx *c)
 {
     c->mi = MortonImage{};
-    auto bits = [](int n) {
-        int b = 0;
-        while ((1ll << b) < n) b++;
-        return b;
-    };
-    const int bx = bits(c->nx), by = bits(c->ny), bz = bits(c->nz);
-    const int total = bx + by + bz;
-    if (total > 32) return RWNMR_OK;
-    const uint64_t padded = 1ull << total;
-    if (padded > 4ull * (uint64_t)c->nx * c->ny * c->nz) return RWNMR_OK;
-    MortonImage m;
-    int pos = 0;
-    for (int i = 0; i < std::max(bx, std::max(by, bz)); i++)
-    {
-        if (i < bx) m.mx |= 1u << pos++;
-        if (i < by) m.my |= 1u << pos++;
-        if (i < bz) m.mz |= 1u << pos++;
-    }
-    m.ex = dilate_bits((uint32_t)c->nx - 1, m.mx);
-    m.ey = dilate_bits((uint32_t)c->ny - 1, m.my);
-    m.ez = dilate_bits((uint32_t)c->nz - 1, m.mz);
-    const uint32_t n_words = (uint32_t)std::max<uint64_t>(1, padded >> 5);
+    uint32_t n_words = 0;
+    MortonImage m = morton_params(c->nx, c->ny, c->nz, n_words);
+    if (!n_words) return RWNMR_OK;
     if (c->morton.ensure((size_t)n_words * c->words) != cudaSuccess)
     {
         cudaGetLastError(); // no room for the copy: the walks use the bit-block layout

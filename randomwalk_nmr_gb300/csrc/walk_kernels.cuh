@@ -1,5 +1,6 @@
 // Launch-argument structs and launchers shared by walk_kernels.cu and engine.cu.
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -133,6 +134,37 @@ cudaError_t walker_order(const int32_t *x, const int32_t *y, const int32_t *z, i
 // x0[k] = ux[perm[k]] (and y, z, seeds)
 cudaError_t gather_walkers(const int32_t *perm, int64_t n, const int32_t *ux, const int32_t *uy, const int32_t *uz,
                            const uint64_t *us, int32_t *x0, int32_t *y0, int32_t *z0, uint64_t *s0, cudaStream_t s);
+// Morton parameters of an nx x ny x nz image (words = 0: no Morton copy). A copy is made when the
+// power-of-two box around the image holds at most four times its voxels and its index fits 32 bits;
+// the lowest index bits cycle x, y, z.
+inline MortonImage morton_params(int nx, int ny, int nz, uint32_t &n_words)
+{
+    MortonImage m;
+    n_words = 0;
+    auto bits = [](int n) {
+        int b = 0;
+        while ((1ll << b) < n) b++;
+        return b;
+    };
+    const int bx = bits(nx), by = bits(ny), bz = bits(nz);
+    const int total = bx + by + bz;
+    if (total > 32) return m;
+    const uint64_t padded = 1ull << total;
+    if (padded > 4ull * (uint64_t)nx * ny * nz) return m;
+    int pos = 0;
+    for (int i = 0; i < std::max(bx, std::max(by, bz)); i++)
+    {
+        if (i < bx) m.mx |= 1u << pos++;
+        if (i < by) m.my |= 1u << pos++;
+        if (i < bz) m.mz |= 1u << pos++;
+    }
+    m.ex = dilate_bits((uint32_t)nx - 1, m.mx);
+    m.ey = dilate_bits((uint32_t)ny - 1, m.my);
+    m.ez = dilate_bits((uint32_t)nz - 1, m.mz);
+    n_words = (uint32_t)std::max<uint64_t>(1, padded >> 5);
+    return m;
+}
+
 // Builds the Morton copy im.mi describes (n_words x W uint32) from im's bit-blocks.
 cudaError_t launch_morton_build(const DevImage &im, int W, uint32_t n_words, uint32_t *out, cudaStream_t s);
 cudaError_t launch_pack_blocks(const uint8_t *labels, int nx, int ny, int nz, int bcols, int brows, int64_t nblocks,
