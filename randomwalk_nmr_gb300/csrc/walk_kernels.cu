@@ -77,7 +77,10 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
     constexpr int NG = PACK ? 1 : NP; // collision-count words per echo
     constexpr int KK = 3 + NG;        // values kept per echo
     constexpr int K = 3 + NP;         // values per echo in the accumulators
-    __shared__ unsigned long long sacc[32 * K];
+    constexpr int KP = KK <= 4 ? 4 : 8; // KK padded to whole 16-byte stores
+    // each warp's sums of the current 32-echo window, [warp][echo][value]: lane 0 stores them after
+    // the reductions, the CTA adds the warps up when the window is flushed
+    __shared__ __align__(16) uint32_t wsum[kWalkThreads / 32][32][KP];
     __shared__ uint4 sdir[6]; // MORTON: direction table
     if (MORTON && threadIdx.x < 6) sdir[threadIdx.x] = morton_direction(im.mi, threadIdx.x);
 
@@ -123,7 +126,6 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
         ew = L.from_initial ? 1.0 : L.wenergy[i];
     }
 
-    for (int k = threadIdx.x; k < 32 * K; k += blockDim.x) sacc[k] = 0;
 
     uint64_t efx = 0;
     if (active && L.record) efx = WF ? walker_fx(ew) : energy_fx<NP>(L.tfx, L.tstride, c);
@@ -145,9 +147,6 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
     for (int e0 = L.e_begin; e0 < L.e_end; e0 += 32)
     {
         const int e1 = min(e0 + 32, L.e_end);
-        uint32_t keep[KK];
-#pragma unroll
-        for (int k = 0; k < KK; k++) keep[k] = 0;
         for (int e = e0; e < e1; e++)
         {
             uint32_t g[NG]; // collisions gained this echo, per phase (PACK: 16 bits per phase)
@@ -203,43 +202,37 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
             }
             if (L.record)
             {
-                const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
-                const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((efx >> 21) & M21));
-                const uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
-                const bool mine = lane == (e - e0);
-                keep[0] = mine ? r0 : keep[0];
-                keep[1] = mine ? r1 : keep[1];
-                keep[2] = mine ? r2 : keep[2];
+                uint32_t r[KP];
+                r[0] = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
+                r[1] = __reduce_add_sync(FULL, (uint32_t)((efx >> 21) & M21));
+                r[2] = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
 #pragma unroll
-                for (int k = 0; k < NG; k++)
+                for (int k = 0; k < NG; k++) r[3 + k] = __reduce_add_sync(FULL, g[k]);
+#pragma unroll
+                for (int k = 3 + NG; k < KP; k++) r[k] = 0;
+                if (lane == 0)
                 {
-                    const uint32_t rg = __reduce_add_sync(FULL, g[k]);
-                    keep[3 + k] = mine ? rg : keep[3 + k];
+                    uint4 *slot = reinterpret_cast<uint4 *>(&wsum[threadIdx.x >> 5][e - e0][0]);
+#pragma unroll
+                    for (int v = 0; v < KP / 4; v++) slot[v] = make_uint4(r[4 * v], r[4 * v + 1], r[4 * v + 2], r[4 * v + 3]);
                 }
             }
         }
         if (L.record)
         {
-            // lane l holds this warp's sums for echo e0 + l
-            if (lane < e1 - e0)
-            {
-                unsigned long long *sa = &sacc[lane * K];
-#pragma unroll
-                for (int k = 0; k < 3; k++)
-                    if (keep[k]) atomicAdd(&sa[k], (unsigned long long)keep[k]);
-#pragma unroll
-                for (int q = 0; q < NP; q++)
-                {
-                    const uint32_t v = PACK ? (keep[3] >> (16 * q)) & 0xffffu : keep[3 + q];
-                    if (v) atomicAdd(&sa[3 + q], (unsigned long long)v);
-                }
-            }
             __syncthreads();
             for (int k = threadIdx.x; k < (e1 - e0) * K; k += blockDim.x)
             {
-                unsigned long long v = sacc[k];
-                if (v) atomicAdd(&L.acc[(size_t)(e0 + 1 + k / K) * K + (k % K)], v);
-                sacc[k] = 0;
+                const int er = k / K, kk = k % K;
+                unsigned long long v = 0;
+#pragma unroll
+                for (int w = 0; w < kWalkThreads / 32; w++)
+                {
+                    const uint32_t x = kk < 3 ? wsum[w][er][kk]
+                                              : (PACK ? (wsum[w][er][3] >> (16 * (kk - 3))) & 0xffffu : wsum[w][er][kk]);
+                    v += x;
+                }
+                if (v) atomicAdd(&L.acc[(size_t)(e0 + 1 + er) * K + kk], v);
             }
             __syncthreads();
         }
