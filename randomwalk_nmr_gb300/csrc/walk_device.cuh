@@ -408,9 +408,8 @@ __device__ __forceinline__ void morton_step(const MortonImage &mi, const uint4 *
 // the per-phase tables, each table[n] = round(f^n * 2^63) with f^n the FP64 repeated product.
 __device__ __forceinline__ uint64_t fx_mul(uint64_t a, uint64_t b)
 {
-    uint64_t hi = __umul64hi(a, b);
-    uint64_t lo = a * b;
-    return (hi << 1) | (lo >> 63);
+    // floor(a b / 2^63) = floor(2a b / 2^64) for a < 2^63; a = 2^63 (the value 1) returns b
+    return a >> 63 ? b : __umul64hi(a << 1, b);
 }
 
 template <int NP>

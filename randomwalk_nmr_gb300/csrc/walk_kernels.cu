@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     bool active = i < st.n;
+    const bool rec = SPE > 0 || L.record; // the fixed-step instances only run recorded walks
 
     WalkerPos p{};
     uint64_t seed = 0;
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                         changed |= g[q] != 0;
                     }
                 }
-                if (changed && L.record)
+                if (changed && rec)
                 {
                     if (WF)
                     {
@@ -200,7 +201,7 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                     }
                 }
             }
-            if (L.record)
+            if (rec)
             {
                 uint32_t r[KP];
                 r[0] = __reduce_add_sync(FULL, (uint32_t)(efx & M21));
@@ -218,7 +219,7 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                 }
             }
         }
-        if (L.record)
+        if (rec)
         {
             __syncthreads();
             for (int k = threadIdx.x; k < (e1 - e0) * K; k += blockDim.x)
