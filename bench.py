@@ -541,11 +541,11 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
+    torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
     from randomwalk_nmr_gb300 import Engine, fx_to_float
 
     res, spe, f = derived(w)
@@ -587,6 +587,8 @@ def main():
             out = walk()
             kernel_s.append(eng.last_kernel_ms * 1e-3)
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
     if dist and not field:
         from randomwalk_nmr_gb300.shard import combine_cpmg
 
