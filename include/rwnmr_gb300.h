@@ -75,10 +75,14 @@ rwnmr_status rwnmr_image_upload_labels(rwnmr_ctx *ctx, const uint8_t *labels, in
                                        int32_t n_phases);
 /* Reads back the packed bit-blocks (ceil(nx/4)*ceil(ny/4)*ceil(nz/4) words). */
 rwnmr_status rwnmr_image_download_blocks(rwnmr_ctx *ctx, uint64_t *blocks);
-/* 1 if the uploaded image also has a Morton (bit-interleaved) copy, which the noflux CPMG walk
- * without voxel division uses (built when the power-of-two box around the image holds at most four
- * times its voxels); 0 otherwise. Results do not depend on it. */
+/* 1 if the uploaded image also has a Morton (bit-interleaved) copy, which the noflux walks without
+ * voxel division use (CPMG, PFGSE, the adjoint; built when the power-of-two box around the image
+ * holds at most four times its voxels or the copy takes at most 48 MB); 0 otherwise. Results do not
+ * depend on it. */
 int32_t rwnmr_image_layout(const rwnmr_ctx *ctx);
+/* allow_morton = 0: later image uploads build no Morton copy (saves its memory; the walks then use
+ * the bit-blocks). Default 1. No counterpart in the reference. */
+rwnmr_status rwnmr_ctx_set_image_layout(rwnmr_ctx *ctx, int32_t allow_morton);
 
 /* ---- walkers --------------------------------------------------------------------------- */
 /* Initial state (Walker::initialPosition / initialSeed). Positions are in walk units (voxels

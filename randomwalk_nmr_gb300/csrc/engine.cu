@@ -87,6 +87,7 @@ struct rwnmr_ctx
     DevBuf<uint8_t> labels;
     DevBuf<uint32_t> morton; // Morton copy of the image for the noflux walk (mi.words null: none)
     MortonImage mi;
+    bool allow_morton = true; // build the Morton copy at upload (rwnmr_ctx_set_image_layout)
 
     int64_t n = 0;
     bool has_walkers = false;
@@ -328,8 +329,14 @@ static rwnmr_status set_dims(rwnmr_ctx *c, int32_t nx, int32_t ny, int32_t nz, i
 static rwnmr_status build_morton(rwnmr_ctx *c)
 {
     c->mi = MortonImage{};
+    if (!c->allow_morton)
+    {
+        c->morton.release();
+        return RWNMR_OK;
+    }
     uint32_t n_words = 0;
-    MortonImage m = morton_params(c->nx, c->ny, c->nz, n_words);
+    // padded copies of up to 48 MB stay L2-resident on GB300 (the padding is never touched)
+    MortonImage m = morton_params(c->nx, c->ny, c->nz, n_words, c->words, 48ull << 20);
     if (!n_words) return RWNMR_OK;
     if (c->morton.ensure((size_t)n_words * c->words) != cudaSuccess)
     {
@@ -347,6 +354,13 @@ static rwnmr_status build_morton(rwnmr_ctx *c)
 }
 
 int32_t rwnmr_image_layout(const rwnmr_ctx *c) { return c && c->has_image && c->mi.words ? 1 : 0; }
+
+rwnmr_status rwnmr_ctx_set_image_layout(rwnmr_ctx *c, int32_t allow_morton)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    c->allow_morton = allow_morton != 0;
+    return RWNMR_OK;
+}
 
 rwnmr_status rwnmr_image_upload_labels(rwnmr_ctx *c, const uint8_t *labels, int32_t nx, int32_t ny, int32_t nz,
                                        int32_t n_phases)

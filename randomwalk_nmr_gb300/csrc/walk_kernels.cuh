@@ -134,10 +134,11 @@ cudaError_t walker_order(const int32_t *x, const int32_t *y, const int32_t *z, i
 // x0[k] = ux[perm[k]] (and y, z, seeds)
 cudaError_t gather_walkers(const int32_t *perm, int64_t n, const int32_t *ux, const int32_t *uy, const int32_t *uz,
                            const uint64_t *us, int32_t *x0, int32_t *y0, int32_t *z0, uint64_t *s0, cudaStream_t s);
-// Morton parameters of an nx x ny x nz image (words = 0: no Morton copy). A copy is made when the
-// power-of-two box around the image holds at most four times its voxels and its index fits 32 bits;
-// the lowest index bits cycle x, y, z.
-inline MortonImage morton_params(int nx, int ny, int nz, uint32_t &n_words)
+// Morton parameters of an nx x ny x nz image (words = 0: no Morton copy). A copy is made when its
+// index fits 32 bits and the power-of-two box around the image holds at most four times its voxels
+// or, with max_bytes > 0, when the copy (W words per 32 voxels) takes at most max_bytes; the lowest
+// index bits cycle x, y, z.
+inline MortonImage morton_params(int nx, int ny, int nz, uint32_t &n_words, int W = 1, uint64_t max_bytes = 0)
 {
     MortonImage m;
     n_words = 0;
@@ -150,7 +151,8 @@ inline MortonImage morton_params(int nx, int ny, int nz, uint32_t &n_words)
     const int total = bx + by + bz;
     if (total > 32) return m;
     const uint64_t padded = 1ull << total;
-    if (padded > 4ull * (uint64_t)nx * ny * nz) return m;
+    const bool small = max_bytes > 0 && (padded / 32) * 4 * (uint64_t)W <= max_bytes;
+    if (padded > 4ull * (uint64_t)nx * ny * nz && !small) return m;
     int pos = 0;
     for (int i = 0; i < std::max(bx, std::max(by, bz)); i++)
     {

@@ -33,7 +33,7 @@ STATUS = {
 EXPORTS = [
     "rwnmr_ctx_create", "rwnmr_ctx_destroy", "rwnmr_last_error", "rwnmr_version", "rwnmr_ctx_set_stream",
     "rwnmr_ctx_launch_count", "rwnmr_ctx_last_kernel_ms", "rwnmr_image_upload", "rwnmr_image_upload_labels",
-    "rwnmr_image_download_blocks", "rwnmr_image_layout", "rwnmr_walkers_upload", "rwnmr_walkers_download", "rwnmr_cpmg_run",
+    "rwnmr_image_download_blocks", "rwnmr_image_layout", "rwnmr_ctx_set_image_layout", "rwnmr_walkers_upload", "rwnmr_walkers_download", "rwnmr_cpmg_run",
     "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_map_continue", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
     "rwnmr_cpmg_run_noalloc", "rwnmr_batch_create", "rwnmr_batch_destroy", "rwnmr_batch_last_error",
     "rwnmr_batch_last_kernel_ms", "rwnmr_batch_launch_count", "rwnmr_batch_add_image", "rwnmr_batch_cpmg",
@@ -163,8 +163,12 @@ class Engine:
 
     @property
     def morton_layout(self) -> bool:
-        """True if the uploaded image has the Morton copy the noflux CPMG walk uses."""
+        """True if the uploaded image has the Morton copy the noflux walks use."""
         return bool(self.lib.rwnmr_image_layout(self.ctx))
+
+    def allow_morton(self, allow: bool = True):
+        """Whether later image uploads build the Morton copy (default True)."""
+        self._check(self.lib.rwnmr_ctx_set_image_layout(self.ctx, int(bool(allow))))
 
     def set_stream(self, stream_ptr: int | None):
         self._check(self.lib.rwnmr_ctx_set_stream(self.ctx, _vp(stream_ptr or 0)))

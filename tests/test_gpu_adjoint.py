@@ -10,10 +10,11 @@ from randomwalk_nmr_gb300 import host
 pytestmark = pytest.mark.gpu
 
 
-def setup(engine, n_phases, seed=12, n=3000):
+def setup(engine, n_phases, seed=12, n=3000, morton=True):
     lab, _ = host.synth_spheres((24, 28, 22), 2.0, 5.0, 0.4, n_phases, seed=seed)
     blocks, _ = host.pack_blocks(lab)
     x, y, z, s, _ = host.place_walkers(blocks, lab.shape, n, seed)
+    engine.allow_morton(morton)
     engine.upload_labels(lab, n_phases)
     engine.upload_walkers(x, y, z, s)
     return lab, (x, y, z, s)
@@ -41,9 +42,9 @@ def pathwise_gradient(oracle, lab, w, n_echoes, spe, f, grad, n_phases):
     return out
 
 
-@pytest.mark.parametrize("n_phases", [1, 2])
-def test_adjoint_matches_pathwise_and_finite_differences(engine, oracle, n_phases):
-    lab, w = setup(engine, n_phases)
+@pytest.mark.parametrize("n_phases,morton", [(1, True), (2, True), (2, False)])
+def test_adjoint_matches_pathwise_and_finite_differences(engine, oracle, n_phases, morton):
+    lab, w = setup(engine, n_phases, morton=morton)
     n_echoes, spe = 60, 2
     f = dfactor([10.0, 30.0][:n_phases])
     rng = np.random.default_rng(0)

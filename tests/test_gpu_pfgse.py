@@ -11,11 +11,13 @@ pytestmark = pytest.mark.gpu
 ATT_TOL = 1e-12
 
 
-def setup(engine, seed=3, n=4000, shape=(30, 26, 28), n_phases=1):
+def setup(engine, seed=3, n=4000, shape=(30, 26, 28), n_phases=1, morton=True):
     lab, _ = host.synth_spheres(shape, 2.0, 6.0, 0.4, n_phases, seed=seed)
     blocks, _ = host.pack_blocks(lab)
     x, y, z, s, _ = host.place_walkers(blocks, lab.shape, n, seed + 100)
+    engine.allow_morton(morton)
     engine.upload_labels(lab, n_phases)
+    assert engine.morton_layout == morton
     engine.upload_walkers(x, y, z, s)
     return lab, (x, y, z, s)
 
@@ -31,10 +33,10 @@ def kvecs(n_g, gmax, pulse_ms=1.0, gamma=42.576 * 2 * np.pi):
     return np.array(out)
 
 
-@pytest.mark.parametrize("bc", ["noflux", "periodic", "mirror"])
+@pytest.mark.parametrize("bc,morton", [("noflux", True), ("noflux", False), ("periodic", True), ("mirror", True)])
 @pytest.mark.parametrize("gdir", [(0, 0, 100.0), (60.0, 0, 0), (30.0, 40.0, 20.0)])
-def test_pfgse_parity(engine, oracle, bc, gdir):
-    lab, w = setup(engine)
+def test_pfgse_parity(engine, oracle, bc, morton, gdir):
+    lab, w = setup(engine, morton=morton)
     steps = np.array([15, 40, 100, 250], np.int32)
     kv = kvecs(16, gdir)
     f = dfactor(10.0)
