@@ -294,9 +294,9 @@ __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
         __syncthreads();
         unsigned *H = L.hist + img.hist0;
         const int spe = L.steps_per_echo;
-        for (int e = 0; e <= L.n_echoes; e++)
+        int64_t row = 0; // hist_row(e), stepped: row(e + 1) = row(e) + spe * e + 1
+        for (int e = 0; e <= L.n_echoes; row += (int64_t)spe * e + 1, e++)
         {
-            const int64_t row = hist_row(e, spe);
 #pragma unroll
             for (int j = 0; j < WPT; j++)
                 if (active[j])
