@@ -115,7 +115,7 @@ struct rwnmr_ctx
     int field_mode = 0;
     double field_dg = 0.0;
     int field_axis = 0;
-    DevBuf<double> field, phase;
+    DevBuf<double> field, phase, btab;
 
     rwnmr_status fail(rwnmr_status s, const char *fmt, ...)
     {
@@ -281,6 +281,7 @@ void rwnmr_ctx_destroy(rwnmr_ctx *c)
     c->tfx.release(); c->tfp.release(); c->acc.release(); c->hist.release(); c->status.release();
     c->grad.release(); c->partial.release(); c->partial_g.release(); c->kbuf.release(); c->Mbuf.release();
     c->gbuf.release(); c->ibuf.release(); c->disp.release(); c->energy.release();
+    c->wf.release(); c->wenergy.release(); c->field.release(); c->phase.release(); c->btab.release();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -708,6 +709,14 @@ rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p
     L.field = c->field_mode == 2 ? c->field.p : nullptr;
     L.dg = c->field_dg;
     L.axis = c->field_axis;
+    if (c->field_mode == 1)
+    {
+        const int na = c->field_axis == 0 ? c->nx : (c->field_axis == 1 ? c->ny : c->nz);
+        RW_CUDA(c, c->btab.ensure((size_t)na), "field table");
+        RW_CUDA(c, launch_field_table(c->field_dg, na, c->btab.p, c->stream), "field table");
+        c->launches++;
+        L.btab = c->btab.p;
+    }
     L.phase = c->phase.p;
     L.acc = c->acc.p;
     L.status = c->status.p;

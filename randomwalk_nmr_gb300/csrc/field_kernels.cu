@@ -43,14 +43,39 @@ __device__ __forceinline__ double field_at(const DevImage &im, const WalkerPos &
         // a walker only ever moves into pore voxels; only its start voxel can be solid
         if (may_be_solid && voxel_solid<W>(im, ix, iy, iz)) return 0.0;
         const int coord = L.axis == 0 ? ix : (L.axis == 1 ? iy : iz);
-        return (double)coord * L.dg;
+        return __ldg(L.btab + coord); // (double)coord * dg, tabulated: a load instead of FP64 work
     }
     return __ldg(L.field + ((int64_t)ix + (int64_t)iy * im.nx + (int64_t)iz * im.nx * im.ny));
 }
 
+// round(e * 2^61) + 2^61 for |e| <= 1, round half to even, in integer arithmetic: the mantissa shifted
+// by the exponent (the FP64 pipe is this kernel's bound; its integer ALU is nearly idle).
 __device__ __forceinline__ uint64_t energy_offset_fx(double e)
 {
-    return (uint64_t)(__double2ll_rn(e * 0x1p61) + (1ll << 61));
+    const long long bits = __double_as_longlong(e);
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    uint64_t mag = 0;
+    if (ex != 0)
+    {
+        const uint64_t mant = ((uint64_t)bits & ((1ull << 52) - 1)) | (1ull << 52);
+        const int sh = ex - 1014; // e * 2^61 = mant * 2^(ex - 1075 + 61)
+        if (sh >= 0)
+            mag = mant << sh;
+        else if (sh > -64)
+        {
+            const int r = -sh;
+            const uint64_t q = mant >> r, rem = mant & ((1ull << r) - 1), half = 1ull << (r - 1);
+            mag = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+        }
+    }
+    const long long v = bits < 0 ? -(long long)mag : (long long)mag;
+    return (uint64_t)(v + (1ll << 61));
+}
+
+__global__ void field_table_kernel(double dg, int n, double *__restrict__ btab)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) btab[k] = (double)k * dg;
 }
 } // namespace
 
@@ -213,6 +238,12 @@ void with_bc_field(int bc_key, F &&f)
     }
 }
 } // namespace
+
+cudaError_t launch_field_table(double dg, int n, double *btab, cudaStream_t s)
+{
+    field_table_kernel<<<(n + 255) / 256, 256, 0, s>>>(dg, n, btab);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_cpmg_field(int bc_key, int np, bool uniform, const DevImage &im, const WalkState &st,
                               const FieldLaunch &L, dim3 grid, cudaStream_t s)

@@ -54,6 +54,7 @@ struct FieldLaunch
     double gammatau;         // 0.5 * gamma * time interval
     const double *field;     // array field [nz][ny][nx]
     double dg;               // uniform field: value per voxel along `axis` (0 in solid voxels)
+    const double *btab;      // uniform field: btab[k] = k * dg for the image coordinates k along `axis`
     int axis;
     double *phase;           // [n] walker phases, carried across launches
     const double *wf;        // per-walker decrease factors [n] (single phase), or null for the tables
@@ -120,6 +121,8 @@ cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkS
                              dim3 grid, cudaStream_t s);
 cudaError_t launch_cpmg_field(int bc_key, int np, bool uniform, const DevImage &im, const WalkState &st,
                               const FieldLaunch &L, dim3 grid, cudaStream_t s);
+// btab[k] = (double)k * dg, k < n (the uniform field along one axis, as cpmg_field_kernel evaluates it)
+cudaError_t launch_field_table(double dg, int n, double *btab, cudaStream_t s);
 cudaError_t launch_cpmg_adjoint(int bc_key, int np, const DevImage &im, const WalkState &st, const AdjointLaunch &L,
                                 dim3 grid, cudaStream_t s);
 cudaError_t launch_pfgse_walk(int bc_key, int np, const DevImage &im, const WalkState &st, const PfgseLaunch &L,
