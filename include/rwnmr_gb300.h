@@ -165,11 +165,14 @@ typedef struct rwnmr_field_cpmg_params
  * energy after an echo is (prod over phases of f_p^collisions) * cos(phase). Outputs (nullable):
  *   echo_sum  [n_echoes+1] energy sums (index 0 = initial), each walker's energy rounded to a
  *             multiple of 2^-61 and summed exactly
+ *   echo_fx   [n_echoes+1][3] the exact sums behind echo_sum: limbs l0, l1, l2 of
+ *             S = sum over walkers of (E * 2^61 + 2^61), S = l0 + l1 * 2^21 + l2 * 2^42
+ *             (echo_sum = (S - n * 2^61) * 2^-61)
  *   phase_out [n]          final phase of every walker
  * Final positions, seeds and collision counts are left in the context (rwnmr_walkers_download).
  * Requires a field set by rwnmr_field_set_uniform or rwnmr_field_upload. */
 rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *ctx, const rwnmr_field_cpmg_params *p, double *echo_sum,
-                                  double *phase_out);
+                                  uint64_t *echo_fx, double *phase_out);
 
 /* ---- CPMG walk without allocation ------------------------------------------------------ */
 /* No counterpart in the reference (its CUDA path cudaMallocs its buffers on every run).

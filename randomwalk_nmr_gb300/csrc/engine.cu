@@ -664,7 +664,8 @@ rwnmr_status rwnmr_field_clear(rwnmr_ctx *c)
     return RWNMR_OK;
 }
 
-rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p, double *echo_sum, double *phase_out)
+rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p, double *echo_sum, uint64_t *echo_fx,
+                                  double *phase_out)
 {
     RW_TRY(need_run_state(c));
     if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
@@ -685,10 +686,10 @@ rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p
         RW_CUDA(c, c->wenergy.ensure((size_t)std::max<int64_t>(c->n, 1)), "walker survival probabilities");
     else
     {
-        std::vector<double> t;
-        build_tables(p->dfactor, c->n_phases, slots, nmax, &t, nullptr);
-        RW_CUDA(c, c->tfp.ensure(t.size()), "tables");
-        RW_CUDA(c, cudaMemcpyAsync(c->tfp.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables upload");
+        std::vector<uint64_t> fx;
+        build_tables(p->dfactor, c->n_phases, slots, nmax, nullptr, &fx);
+        RW_CUDA(c, c->tfx.ensure(fx.size()), "tables");
+        RW_CUDA(c, cudaMemcpyAsync(c->tfx.p, fx.data(), fx.size() * 8, cudaMemcpyHostToDevice, c->stream), "tables upload");
     }
     RW_CUDA(c, c->acc.ensure((size_t)(p->n_echoes + 1) * K), "echo accumulators");
     RW_CUDA(c, c->phase.ensure((size_t)std::max<int64_t>(c->n, 1)), "walker phases");
@@ -701,7 +702,7 @@ rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p
     const WalkState st = c->state();
     FieldLaunch L{};
     L.steps_per_inversion = spi;
-    L.t = per_walker ? nullptr : c->tfp.p;
+    L.tfx = per_walker ? nullptr : c->tfx.p;
     L.tstride = (int)(nmax + 1);
     L.wf = per_walker ? c->wf.p : nullptr;
     L.palive = per_walker ? c->wenergy.p : nullptr;
@@ -753,9 +754,11 @@ rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->last_ms = ms;
+    if (echo_fx)
+        for (size_t k = 0; k < acc.size(); k++) echo_fx[k] = acc[k];
     if (echo_sum)
     {
-        // every walker added round(E * 2^61) + 2^61
+        // every walker added E * 2^61 + 2^61
         const __int128 offset = (__int128)c->n << 61;
         for (int e = 0; e <= p->n_echoes; e++)
         {

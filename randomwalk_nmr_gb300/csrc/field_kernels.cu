@@ -14,9 +14,16 @@
 //   * B at the walker's voxel lives in a register and is refreshed only after a move; the
 //     uniform field (coord * dG in pore voxels, 0 in solid ones) is evaluated in place rather
 //     than gathered from an 8-byte-per-voxel array;
-//   * energies are signed: each walker adds round(E * 2^61) + 2^61, in [0, 2^62], as three 21-bit
-//     limbs through redux.sync (the same echo-transposed accumulation as the plain CPMG walk), and
-//     the host subtracts n * 2^61. Sums are exact integers, identical run to run.
+//   * energies are signed: each walker adds E * 2^61 + 2^61, in [0, 2^62], as three 21-bit limbs
+//     through redux.sync (the same echo-transposed accumulation as the plain CPMG walk), and the host
+//     subtracts n * 2^61. Sums are exact integers, identical run to run;
+//   * the only FP64 arithmetic per echo is the reference's phase updates (two FMAs per step, kept bit
+//     for bit). E = pAlive * cos(phase) is evaluated in 64-bit integer arithmetic, since FP64 is the
+//     slow pipe of this GPU and its integer pipes are nearly idle here: pAlive from the fixed-point
+//     survival tables (or the per-walker FP64 product converted exactly), cos(phase) by a fixed-point
+//     Payne-Hanek-style reduction to turns, a 64-entry quadrant table and Taylor terms. The absolute
+//     error of E is below 2^-59 for |phase| < 2^40 (the reference's FP64 cos itself rounds at up to
+//     2^-53); larger or non-finite phases take CUDA's cos.
 #include <cstdint>
 #include <type_traits>
 #include <cuda_runtime.h>
@@ -72,6 +79,83 @@ __device__ __forceinline__ uint64_t energy_offset_fx(double e)
     return (uint64_t)(v + (1ll << 61));
 }
 
+#include "cos_table.inc"
+
+// cos(phase) * 2^62 as a signed integer, for |phase| < 2^40 (false otherwise: larger, inf, nan).
+//   1. theta = |phase| / (2 pi) mod 1 in units of 2^-64 turns: the 53-bit mantissa times 2^128 / (2 pi)
+//      (two words) and the exponent's window of the product (the idea of Payne and Hanek's reduction,
+//      a fixed window of the constant being enough below 2^40); error below 2 units.
+//   2. k = theta rounded to 1/256 turn, r = 2 pi (theta - k / 256) with |r| <= pi / 256.
+//   3. cos(k pi / 128 + r) from the quadrant k / 64, the table cos / sin (j pi / 128), j = k mod 64,
+//      and cos r = 1 - r^2/2 + r^4/24 - r^6/720, sin r = r - r^3/6 + r^5/120 - r^7/5040 (the next
+//      terms are below 2^-66), every product a 64-bit high multiply at a scale chosen per term.
+// Measured against exact values (cos_table.py's 256-bit arithmetic): error below 4 units of 2^-62.
+__device__ __forceinline__ bool cos_q62(double phase, const ulonglong2 *__restrict__ quad, long long &out)
+{
+    const uint64_t bits = (uint64_t)__double_as_longlong(phase);
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    if (ex >= 1063) return false;
+    const int sh = 1139 - ex; // theta = (mantissa * 2^128 / (2 pi)) >> sh, modulo 2^64
+    uint64_t theta = 0;
+    if (ex != 0 && sh < 178)
+    {
+        const uint64_t m = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+        const uint64_t lo2 = m * INV_2PI_HI;
+        const uint64_t q1 = __umul64hi(m, INV_2PI_LO) + lo2;
+        const uint64_t q2 = __umul64hi(m, INV_2PI_HI) + (q1 < lo2 ? 1 : 0);
+        theta = sh < 128 ? (q1 >> (sh - 64)) | (q2 << (128 - sh)) : q2 >> (sh - 128);
+    }
+    const uint64_t tr = theta + (1ull << 55);
+    const int k = (int)(tr >> 56);
+    const long long d = (long long)(theta - (tr & ~((1ull << 56) - 1))); // [-2^55, 2^55)
+    const bool neg_r = d < 0;
+    const uint64_t a = (uint64_t)(neg_r ? -d : d);
+    const uint64_t R = __umul64hi(a << 8, TWO_PI_Q61); // |r| 2^69
+    const uint64_t u = __umul64hi(R, R);               // r^2 2^74
+    const uint64_t H = C_H24 - __umul64hi(u, C_K720);  // (1/24 - u/720) 2^68
+    const uint64_t G = (1ull << 63) - (__umul64hi(u, H) >> 14);  // (1/2 - u (1/24 - u/720)) 2^64
+    const uint64_t cr = (1ull << 63) - (__umul64hi(u, G) >> 11); // cos r 2^63
+    const uint64_t J = C_J120 - __umul64hi(u, C_K5040);          // (1/120 - u/5040) 2^70
+    const uint64_t I = C_I6 - (__umul64hi(u, J) >> 14);          // (1/6 - u (...)) 2^66
+    const uint64_t S1 = (1ull << 63) - (__umul64hi(u, I) >> 13); // sin r / r 2^63
+    const uint64_t sr = __umul64hi(R, S1);                       // |sin r| 2^68
+    const ulonglong2 cs = quad[k & 63];
+    const bool odd = (k >> 6) & 1;
+    // quadrants 0..3: cos(phi), -sin(phi), -cos(phi), sin(phi) with phi = j pi / 128 + r
+    const long long p1 = (long long)__umul64hi(odd ? cs.y : cs.x, cr);
+    const long long p2 = (long long)(__umul64hi(odd ? cs.x : cs.y, sr) >> 5);
+    const long long v = odd == neg_r ? p1 - p2 : p1 + p2;
+    out = (((k >> 6) + 1) & 2) ? -v : v;
+    return true;
+}
+
+// round(p * 2^63), half to even (the survival tables' rounding), for an FP64 probability p in
+// [0, 1], from its bits.
+__device__ __forceinline__ uint64_t prob_q63(double p)
+{
+    const uint64_t bits = (uint64_t)__double_as_longlong(p);
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    if (ex < 959) return 0; // below 2^-64
+    const uint64_t m = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = ex - 1012; // p 2^63 = m 2^(ex - 1075 + 63), sh <= 11
+    if (sh >= 0) return m << sh;
+    const int r = -sh; // 1 .. 53
+    const uint64_t q = m >> r, rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+    return q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+}
+
+// The echo term E * 2^61 + 2^61 of a walker with survival probability pal63 / 2^63 and phase `phase`.
+// pal_fp64() is the same probability as an FP64 number, used only when cos_q62 declines the phase.
+template <typename PalFp64>
+__device__ __forceinline__ uint64_t echo_term(double phase, uint64_t pal63, PalFp64 &&pal_fp64,
+                                              const ulonglong2 *__restrict__ quad)
+{
+    long long c62;
+    if (!cos_q62(phase, quad, c62)) return energy_offset_fx(pal_fp64() * cos(phase));
+    const uint64_t m = __umul64hi(pal63, (uint64_t)(c62 < 0 ? -c62 : c62)); // pal |cos| 2^61
+    return (uint64_t)((c62 < 0 ? -(long long)m : (long long)m) + (1ll << 61));
+}
+
 __global__ void field_table_kernel(double dg, int n, double *__restrict__ btab)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -88,6 +172,7 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_field_kernel(DevImage im, W
     constexpr int W = WordsPerBlock<NP>::value;
     constexpr int K = 3;
     __shared__ unsigned long long sacc[32 * K];
+    __shared__ ulonglong2 quad[64];
 
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -135,11 +220,16 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_field_kernel(DevImage im, W
     double B = B0;
 
     for (int k = threadIdx.x; k < 32 * K; k += blockDim.x) sacc[k] = 0;
+    for (int k = threadIdx.x; k < 64; k += blockDim.x)
+        quad[k] = make_ulonglong2(kQuadrantCosSin[k][0], kQuadrantCosSin[k][1]);
+    __syncthreads();
+    // pAlive as 2^63 fixed point: the survival tables, or the walker's own FP64 product converted
+    auto pal_q63 = [&]() { return WF ? prob_q63(pa) : energy_fx<NP>(L.tfx, L.tstride, c); };
+    auto pal_fp64 = [&]() { return WF ? pa : ldexp((double)energy_fx<NP>(L.tfx, L.tstride, c), -63); };
     if (L.e_begin == 0)
     {
         // initial energy sum (output index 0)
-        const double pal = WF ? pa : energy_fp64<NP>(L.t, L.tstride, c);
-        const uint64_t u = active ? energy_offset_fx(pal * cos(phase)) : 0;
+        const uint64_t u = active ? echo_term(phase, pal_q63(), pal_fp64, quad) : 0;
         const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(u & M21));
         const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((u >> 21) & M21));
         const uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(u >> 42));
@@ -184,7 +274,7 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_field_kernel(DevImage im, W
                         phase = __fma_rn(L.gammatau, B, phase);
                     }
                 }
-                u = energy_offset_fx((WF ? pa : energy_fp64<NP>(L.t, L.tstride, c)) * cos(phase));
+                u = echo_term(phase, pal_q63(), pal_fp64, quad);
             }
             const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(u & M21));
             const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((u >> 21) & M21));

@@ -503,7 +503,7 @@ bool CpmgSequence::run_simulation(std::string &err)
         p.time_interval = 1.0e-3 * sim.dt; // timeInterval = 1e-3 * NMR.getTimeInterval()
         raw.assign(E + 1, 0.0);
         echo_collisions.assign((size_t)E * sim.img.n_phases, 0); // the field walk records no collisions per echo
-        if (st == RWNMR_OK) st = rwnmr_cpmg_field_run(sim.ctx, &p, raw.data(), nullptr);
+        if (st == RWNMR_OK) st = rwnmr_cpmg_field_run(sim.ctx, &p, raw.data(), nullptr, nullptr);
         if (st != RWNMR_OK)
         {
             err = std::string("CPMG field walk: ") + rwnmr_last_error(sim.ctx);

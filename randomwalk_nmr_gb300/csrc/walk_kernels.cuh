@@ -49,7 +49,7 @@ struct FieldLaunch
     int e_begin, e_end;      // echoes walked by this launch
     int steps_per_inversion; // steps_per_echo / 2
     int from_initial;        // 1: start from (x0, seed0), no collisions, phase 0; 0: continue
-    const double *t;         // [n_phases][tstride] FP64 survival tables
+    const uint64_t *tfx;     // [n_phases][tstride] survival tables, round(f^n * 2^63)
     int tstride;
     double gammatau;         // 0.5 * gamma * time interval
     const double *field;     // array field [nz][ny][nx]

@@ -266,14 +266,17 @@ class Engine:
 
     def cpmg_field(self, n_echoes: int, steps_per_echo: int, dfactor, gamma: float, time_interval: float,
                    bc: str = "noflux", shift: int = 0, echoes_per_launch: int = 0):
-        """CPMG walk in the internal field; returns the echo energy sums and final walker phases."""
+        """CPMG walk in the internal field; returns the echo energy sums, their exact fixed-point
+        form (echo_fx: sum over walkers of E * 2^61 + 2^61, Python ints) and final walker phases."""
         df = self._dfactor(dfactor)
         prm = FieldCpmgParams(BC[bc], int(shift), int(steps_per_echo), int(n_echoes), _dptr(df), float(gamma),
                               float(time_interval), int(echoes_per_launch))
         echo_sum = np.zeros(n_echoes + 1)
+        limbs = np.zeros((n_echoes + 1, 3), np.uint64)
         phase = np.zeros(self.n)
-        self._check(self.lib.rwnmr_cpmg_field_run(self.ctx, ctypes.byref(prm), _p(echo_sum), _p(phase)))
-        return dict(echo_sum=echo_sum, phase=phase)
+        self._check(self.lib.rwnmr_cpmg_field_run(self.ctx, ctypes.byref(prm), _p(echo_sum), _p(limbs), _p(phase)))
+        echo_fx = [int(a) + (int(b) << 21) + (int(c) << 42) for a, b, c in limbs]
+        return dict(echo_sum=echo_sum, echo_fx=echo_fx, phase=phase)
 
     def map(self, steps: int, bc: str = "noflux", shift: int = 0) -> np.ndarray:
         out = np.zeros(self.n, np.uint32)

@@ -1,0 +1,160 @@
+"""The field walk's fixed-point cosine (field_kernels.cu: cos_q62, prob_q63) restated step for step in
+Python integers, against exact values from cos_table.py's 256-bit arithmetic, and the committed
+constant file against its generator. The GPU's own results are checked against the same exact values
+in test_gpu_field.py."""
+import math
+import os
+import random
+import struct
+import sys
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+CSRC = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "randomwalk_nmr_gb300", "csrc")
+sys.path.insert(0, CSRC)
+import cos_table  # noqa: E402
+
+C = cos_table.constants()
+M64 = (1 << 64) - 1
+BOUND_Q62 = 4  # |cos_q62(x) - cos(x) * 2^62| < 4
+
+
+def umulhi(a, b):
+    return (a * b) >> 64
+
+
+def cos_q62(phase):
+    """field_kernels.cu cos_q62, line by line; None where the kernel falls back to CUDA's cos."""
+    bits = struct.unpack("<Q", struct.pack("<d", phase))[0]
+    ex = (bits >> 52) & 0x7FF
+    if ex >= 1063:
+        return None
+    sh = 1139 - ex
+    theta = 0
+    if ex != 0 and sh < 178:
+        m = (bits & ((1 << 52) - 1)) | (1 << 52)
+        lo2 = (m * C["INV_2PI_HI"]) & M64
+        q1 = (umulhi(m, C["INV_2PI_LO"]) + lo2) & M64
+        q2 = (umulhi(m, C["INV_2PI_HI"]) + (1 if q1 < lo2 else 0)) & M64
+        theta = ((q1 >> (sh - 64)) | (q2 << (128 - sh))) & M64 if sh < 128 else q2 >> (sh - 128)
+    tr = (theta + (1 << 55)) & M64
+    k = tr >> 56
+    d = (theta - (tr & ~((1 << 56) - 1))) & M64
+    d = d - (1 << 64) if d >> 63 else d
+    neg_r = d < 0
+    a = -d if neg_r else d
+    R = umulhi((a << 8) & M64, C["TWO_PI_Q61"])
+    u = umulhi(R, R)
+    H = C["C_H24"] - umulhi(u, C["C_K720"])
+    G = (1 << 63) - (umulhi(u, H) >> 14)
+    cr = (1 << 63) - (umulhi(u, G) >> 11)
+    J = C["C_J120"] - umulhi(u, C["C_K5040"])
+    I = C["C_I6"] - (umulhi(u, J) >> 14)
+    S1 = (1 << 63) - (umulhi(u, I) >> 13)
+    sr = umulhi(R, S1)
+    cj, sj = C["table"][k & 63]
+    odd = (k >> 6) & 1
+    p1 = umulhi(sj if odd else cj, cr)
+    p2 = umulhi(cj if odd else sj, sr) >> 5
+    v = p1 - p2 if bool(odd) == neg_r else p1 + p2
+    return -v if ((k >> 6) + 1) & 2 else v
+
+
+def prob_q63(p):
+    """field_kernels.cu prob_q63."""
+    bits = struct.unpack("<Q", struct.pack("<d", p))[0]
+    ex = (bits >> 52) & 0x7FF
+    if ex < 959:
+        return 0
+    m = (bits & ((1 << 52) - 1)) | (1 << 52)
+    sh = ex - 1012
+    if sh >= 0:
+        return m << sh
+    r = -sh
+    q, rem, half = m >> r, m & ((1 << r) - 1), 1 << (r - 1)
+    return q + (1 if rem > half or (rem == half and q & 1) else 0)
+
+
+def exact_cos_q62(phase):
+    """cos(phase) * 2^62 as an exact fraction (256-bit reduction and series)."""
+    fr = Fraction(phase)
+    x = (abs(fr.numerator) << cos_table.BITS) // fr.denominator
+    x %= 2 * cos_table.PI
+    half_pi = cos_table.PI // 2
+    q = x // half_pi
+    c, s = cos_table.cos_sin(x - q * half_pi)
+    return Fraction([c, -s, -c, s][q % 4] << 62, 1 << cos_table.BITS)
+
+
+def test_constant_file_matches_generator():
+    with open(os.path.join(CSRC, "cos_table.inc")) as f:
+        assert f.read() == cos_table.render()
+
+
+def test_generator_constants():
+    assert abs(cos_table.PI / 2 ** cos_table.BITS - math.pi) < 1e-15
+    assert abs(C["TWO_PI_Q61"] / 2.0 ** 61 - 2 * math.pi) < 1e-15
+    assert abs(((C["INV_2PI_HI"] << 64) | C["INV_2PI_LO"]) / 2.0 ** 128 - 1 / (2 * math.pi)) < 1e-17
+    for j, (cv, sv) in enumerate(C["table"]):
+        assert abs(cv / 2.0 ** 63 - math.cos(j * math.pi / 128)) < 1e-15
+        assert abs(sv / 2.0 ** 63 - math.sin(j * math.pi / 128)) < 1e-15
+    assert C["table"][0] == (1 << 63, 0)
+
+
+def phases(n, seed):
+    rng = random.Random(seed)
+    out = [0.0, -0.0, 5e-324, 1e-300, 1e-20, 2.0 ** -62, 1.0, -1.0, math.pi, math.pi / 2, -math.pi / 2,
+           2.0 ** 40 - 1.0, -(2.0 ** 40 - 1.0), 1e6, 12345.678]
+    for _ in range(n):
+        r = rng.random()
+        if r < 0.3:
+            out.append(rng.uniform(-10.0, 10.0))
+        elif r < 0.6:
+            out.append(rng.uniform(-1e4, 1e4))
+        elif r < 0.8:
+            out.append(rng.uniform(-1e11, 1e11))
+        else:  # at the table's and the quadrants' boundaries
+            out.append(rng.randint(-40000, 40000) * math.pi / 256 + rng.uniform(-1e-12, 1e-12))
+    return out
+
+
+def test_fixed_point_cosine_error_bound():
+    worst = Fraction(0)
+    for x in phases(4000, 11):
+        err = abs(cos_q62(x) - exact_cos_q62(x))
+        worst = max(worst, err)
+    assert worst < BOUND_Q62, float(worst)
+
+
+def test_fixed_point_cosine_declines_large_and_nonfinite_phases():
+    for x in (2.0 ** 40, -(2.0 ** 41), 1e300, math.inf, -math.inf, math.nan):
+        assert cos_q62(x) is None
+    assert cos_q62(0.0) == 1 << 62 and cos_q62(5e-324) == 1 << 62
+
+
+def test_probability_conversion_rounds_like_the_tables():
+    rng = np.random.default_rng(2)
+    vals = [0.0, 1.0, 0.5, 2.0 ** -64, 2.0 ** -63, 3 * 2.0 ** -65, 5e-324, np.nextafter(1.0, 0.0)]
+    f = rng.uniform(0.9, 1.0, 50)
+    for fv in f:  # repeated products, as the walk builds them
+        v = 1.0
+        for _ in range(int(rng.integers(1, 3000))):
+            v = v * fv
+        vals.append(v)
+    vals += list(rng.uniform(0.0, 1.0, 200)) + list(2.0 ** rng.uniform(-70, 0, 200))
+    for v in vals:
+        assert prob_q63(float(v)) == round(Fraction(float(v)) * 2 ** 63), v  # round half to even
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_echo_term_error_bound(seed):
+    """E * 2^61 from pAlive * 2^63 and cos * 2^62 (field_kernels.cu echo_term): below 3 units."""
+    rng = random.Random(seed)
+    for x in phases(500, seed):
+        pal = rng.choice([1 << 63, 0, rng.randrange(1 << 63)])
+        c62 = cos_q62(x)
+        m = umulhi(pal, abs(c62))
+        e = -m if c62 < 0 else m
+        assert abs(e - Fraction(pal, 1 << 63) * exact_cos_q62(x) / 2) < 3

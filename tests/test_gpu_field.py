@@ -1,11 +1,15 @@
 """CPMG walk in an internal magnetic field (the reference's RESIDUAL_FIELD uniform / import paths)
 against the CPU oracle: positions, RNG states, collision counts and final phases bit-exact (every
-phase update is one fused multiply-add on both sides), echo sums within 1e-12 * n (the GPU's
-cos() and the C library's differ by a few ulp per walker)."""
+phase update is one fused multiply-add on both sides), echo sums within 1e-12 * n of the oracle's
+FP64 sums (which carry the C library's cos), and the exact integer sums within 3 units of 2^-61 per
+walker of values computed with a 256-bit cosine."""
+from fractions import Fraction
+
 import numpy as np
 import pytest
 
 from conftest import dfactor
+from test_field_cos import exact_cos_q62
 from randomwalk_nmr_gb300 import RwnmrError, host
 
 pytestmark = pytest.mark.gpu
@@ -167,3 +171,52 @@ def test_field_per_walker_dfactor(engine, oracle):
     a = engine.cpmg_field(20, 2, None, GAMMA, TIME_INTERVAL)
     b = engine.cpmg_field(20, 2, f[0], GAMMA, TIME_INTERVAL)
     assert np.array_equal(a["echo_sum"], b["echo_sum"]) and np.array_equal(a["phase"], b["phase"])
+
+
+def _fp64_powers(f, n):
+    """f^k, k = 0..n, as the FP64 repeated product (the survival tables and the per-walker product)."""
+    out = np.empty(n + 1)
+    v = 1.0
+    for k in range(n + 1):
+        out[k] = v
+        v = v * f
+    return out
+
+
+@pytest.mark.parametrize("case", ["one_phase", "two_phases", "per_walker"])
+def test_field_energies_within_fixed_point_bound(engine, oracle, case):
+    """The kernel's exact echo sums against exact values: every walker's E * 2^61 (pAlive from its
+    collision counts, cos from its final phase, both downloaded) within 3 units of pAlive * cos(phase)
+    * 2^61 computed with a 256-bit cosine, so the last echo's integer sum is within 3 n units."""
+    n_phases = 2 if case == "two_phases" else 1
+    lab = image(seed=21, n_phases=n_phases)
+    w = walkers(lab, 900, 8)
+    n = len(w[0])
+    rho = [12.0, 40.0][:n_phases]
+    engine.upload_labels(lab, n_phases)
+    engine.upload_walkers(*w)
+    engine.set_field_uniform(40.0, 2, RES)  # a strong gradient: phases over many radians
+    if case == "per_walker":
+        f = dfactor(np.random.default_rng(5).uniform(2.0, 60.0, n))
+        engine.set_walker_dfactor(f)
+        g = engine.cpmg_field(30, 4, None, GAMMA, TIME_INTERVAL)
+    else:
+        g = engine.cpmg_field(30, 4, dfactor(rho), GAMMA, TIME_INTERVAL)
+    st = engine.download_walkers()
+    assert g["echo_fx"][0] == n << 62  # phase 0, pAlive 1: every walker adds 2^61 + 2^61
+    assert np.ptp(g["phase"]) > 10.0
+    coll = st["collisions"]
+    exact = Fraction(0)
+    if case == "per_walker":
+        for k in range(n):
+            pal = Fraction(float(_fp64_powers(f[k], int(coll[k, 0]))[-1]))
+            exact += pal * exact_cos_q62(float(g["phase"][k])) / 2
+    else:
+        tabs = [_fp64_powers(float(dfactor(r)), int(coll[:, q].max())) for q, r in enumerate(rho)]
+        for k in range(n):
+            pal = Fraction(1)
+            for q in range(n_phases):
+                pal *= Fraction(round(Fraction(float(tabs[q][coll[k, q]])) * 2 ** 63), 2 ** 63)
+            exact += pal * exact_cos_q62(float(g["phase"][k])) / 2
+    err = abs(Fraction(g["echo_fx"][-1] - (n << 61)) - exact)
+    assert err < 3 * n, float(err / n)
