@@ -649,18 +649,27 @@ def main():
     sm_hz = float(clk_sum.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
     issue_peak = 152 * 4 * sm_hz  # warp-instructions per second (4 schedulers per SM)
     inst = counters.get("warp_inst_per_walker_step")
+    cache = ""
+    if counters.get("l1_hit_pct") is not None and counters.get("dram_bytes_per_launch"):
+        cache = " (ncu: %.1f%% L1 hit, %.0f MB DRAM per launch)" % (counters["l1_hit_pct"],
+                                                                   counters["dram_bytes_per_launch"] / 1e6)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": counters.get("dram_bytes_per_launch"), "traffic_unit": "bytes per launch",
                 "launches_per_walk": launches_per_walk, "peak_source": peak_kind,
                 "note": ("achieved = bit-block bytes gathered per walker-step (4 B per block word) x walker-steps / "
-                         "walk-kernel time, against the measured HBM copy peak; the gathers are L2-served "
-                         "(ncu: 95.5% L2 hit, 32 MB DRAM per launch), so the binding roof is instruction issue, "
-                         "reported under 'issue'")}
+                         "walk-kernel time, against the measured HBM copy peak; the gathers are served on chip"
+                         + cache + ", so the binding roof is instruction issue, reported under 'issue'"
+                         + (" and the FP64 pipe, under 'fp64'" if field else ""))}
     if inst:
         ach_issue = (value / world) * inst
         roofline["issue"] = {"achieved_warp_inst_per_s": ach_issue, "peak_warp_inst_per_s": issue_peak,
                              "frac": ach_issue / issue_peak, "warp_inst_per_walker_step": inst,
                              "source": "ncu smsp__inst_executed.sum (profiles/kernel_counters.json)"}
+    if field:
+        # the reference's phase updates: two FP64 fused multiply-adds per step, kept bit for bit
+        roofline["fp64"] = {"dfma_per_walker_step": 2, "achieved_tflops": (value / world) * 2 * 2 / 1e12,
+                            "pipe_active_pct_ncu": counters.get("fp64_pipe_pct"),
+                            "note": "no measured FP64 peak on this pool; ncu's FP64 pipe utilisation is the fraction"}
 
     base = None
     echo_err = None

@@ -44,10 +44,13 @@ def rnd(num, den):
     return (2 * num + den) // (2 * den)
 
 
+QUADRANT = 1024  # table entries per quadrant: |r| <= pi / 4096 after the reduction
+
+
 def constants():
     table = []
-    for j in range(64):  # j * pi / 128, the first quadrant in 1/256-turn steps
-        c, s = cos_sin(PI * j // 128)
+    for j in range(QUADRANT):  # j * pi / 2048: the first quadrant in 1/4096-turn steps
+        c, s = cos_sin(PI * j // (2 * QUADRANT))
         table.append((rnd(c << 63, ONE), rnd(s << 63, ONE)))
     two_pi = 2 * PI
     k = rnd(ONE << 128, two_pi)  # 2^128 / (2 pi)
@@ -56,24 +59,26 @@ def constants():
         INV_2PI_HI=k >> 64,
         INV_2PI_LO=k & ((1 << 64) - 1),
         TWO_PI_Q61=rnd(two_pi << 61, ONE),
-        C_H24=rnd(1 << 68, 24),
-        C_K720=rnd(1 << 58, 720),
-        C_J120=rnd(1 << 70, 120),
-        C_K5040=rnd(1 << 60, 5040),
-        C_I6=rnd(1 << 66, 6),
+        C_INV6=rnd(1 << 32, 6),
+        C_INV3072=rnd(1 << 32, 3072),
+        C_INV15360=rnd(1 << 32, 15360),
     )
 
 
 def render():
     c = constants()
     lines = ["// Generated by cos_table.py (exact integer arithmetic); do not edit.",
-             "// Fixed-point cosine of the field walk: 2^128 / (2 pi) in two words, 2 pi * 2^61, the scaled",
-             "// Taylor coefficients of cos r and sin r, and cos / sin (j pi / 128) * 2^63 for j = 0 .. 63."]
-    for name in ("INV_2PI_HI", "INV_2PI_LO", "TWO_PI_Q61", "C_H24", "C_K720", "C_J120", "C_K5040", "C_I6"):
+             "// Fixed-point cosine of the field walk: 2^128 / (2 pi) in two words, 2 pi * 2^61, the 32-bit",
+             "// reciprocals 2^32 / 6, / 3072, / 15360 of the Taylor terms, and cos / sin (j pi / 2048) * 2^63",
+             f"// for j = 0 .. {QUADRANT - 1}."]
+    for name in ("INV_2PI_HI", "INV_2PI_LO", "TWO_PI_Q61"):
         lines.append(f"constexpr uint64_t {name} = 0x{c[name]:016x}ull;")
-    lines.append("__device__ const uint64_t kQuadrantCosSin[64][2] = {")
-    for j, (cv, sv) in enumerate(c["table"]):
-        lines.append(f"    {{0x{cv:016x}ull, 0x{sv:016x}ull}},  // j = {j}")
+    for name in ("C_INV6", "C_INV3072", "C_INV15360"):
+        lines.append(f"constexpr uint32_t {name} = {c[name]}u;")
+    lines.append(f"constexpr int kQuadrant = {QUADRANT};")
+    lines.append(f"__device__ const uint64_t kQuadrantCosSin[{QUADRANT}][2] = {{")
+    for cv, sv in c["table"]:
+        lines.append(f"    {{0x{cv:016x}ull, 0x{sv:016x}ull}},")
     lines.append("};")
     return "\n".join(lines) + "\n"
 

@@ -21,9 +21,9 @@
 //     for bit). E = pAlive * cos(phase) is evaluated in 64-bit integer arithmetic, since FP64 is the
 //     slow pipe of this GPU and its integer pipes are nearly idle here: pAlive from the fixed-point
 //     survival tables (or the per-walker FP64 product converted exactly), cos(phase) by a fixed-point
-//     Payne-Hanek-style reduction to turns, a 64-entry quadrant table and Taylor terms. The absolute
-//     error of E is below 2^-59 for |phase| < 2^40 (the reference's FP64 cos itself rounds at up to
-//     2^-53); larger or non-finite phases take CUDA's cos.
+//     Payne-Hanek-style reduction to turns, a 1024-entry quadrant table and Taylor terms. The absolute
+//     error of E is below 2^-59.5 for |phase| < 2^40 (the reference's FP64 cos itself rounds at up
+//     to 2^-53); larger or non-finite phases take CUDA's cos.
 #include <cstdint>
 #include <type_traits>
 #include <cuda_runtime.h>
@@ -82,14 +82,14 @@ __device__ __forceinline__ uint64_t energy_offset_fx(double e)
 #include "cos_table.inc"
 
 // cos(phase) * 2^62 as a signed integer, for |phase| < 2^40 (false otherwise: larger, inf, nan).
-//   1. theta = |phase| / (2 pi) mod 1 in units of 2^-64 turns: the 53-bit mantissa times 2^128 / (2 pi)
+//   1. theta = |phase| / (2 pi) mod 1 in units of 2^-66 turns: the 53-bit mantissa times 2^128 / (2 pi)
 //      (two words) and the exponent's window of the product (the idea of Payne and Hanek's reduction,
-//      a fixed window of the constant being enough below 2^40); error below 2 units.
-//   2. k = theta rounded to 1/256 turn, r = 2 pi (theta - k / 256) with |r| <= pi / 256.
-//   3. cos(k pi / 128 + r) from the quadrant k / 64, the table cos / sin (j pi / 128), j = k mod 64,
-//      and cos r = 1 - r^2/2 + r^4/24 - r^6/720, sin r = r - r^3/6 + r^5/120 - r^7/5040 (the next
-//      terms are below 2^-66), every product a 64-bit high multiply at a scale chosen per term.
-// Measured against exact values (cos_table.py's 256-bit arithmetic): error below 4 units of 2^-62.
+//      a fixed window of the constant being enough below 2^40); error below 2^-66 turns.
+//   2. k = theta rounded to 1/4096 turn, r = 2 pi (theta - k / 4096) with |r| <= pi / 4096.
+//   3. cos(k pi / 2048 + r) from the quadrant k / 1024, the table cos / sin (j pi / 2048), j = k mod 1024,
+//      and cos r = 1 - r^2/2 + r^4/24, sin r = r - r^3/6 + r^5/120 (the next terms are below 2^-71):
+//      r and r^2 in 64-bit fixed point, the higher terms in 32-bit multiplies.
+// Measured against exact values (cos_table.py's 256-bit arithmetic): error below 2.1 units of 2^-62.
 __device__ __forceinline__ bool cos_q62(double phase, const ulonglong2 *__restrict__ quad, long long &out)
 {
     const uint64_t bits = (uint64_t)__double_as_longlong(phase);
@@ -97,6 +97,7 @@ __device__ __forceinline__ bool cos_q62(double phase, const ulonglong2 *__restri
     if (ex >= 1063) return false;
     const int sh = 1139 - ex; // theta = (mantissa * 2^128 / (2 pi)) >> sh, modulo 2^64
     uint64_t theta = 0;
+    uint32_t g = 0; // the next two bits of the product (2^-65, 2^-66 turns)
     if (ex != 0 && sh < 178)
     {
         const uint64_t m = (bits & ((1ull << 52) - 1)) | (1ull << 52);
@@ -104,28 +105,30 @@ __device__ __forceinline__ bool cos_q62(double phase, const ulonglong2 *__restri
         const uint64_t q1 = __umul64hi(m, INV_2PI_LO) + lo2;
         const uint64_t q2 = __umul64hi(m, INV_2PI_HI) + (q1 < lo2 ? 1 : 0);
         theta = sh < 128 ? (q1 >> (sh - 64)) | (q2 << (128 - sh)) : q2 >> (sh - 128);
+        g = (uint32_t)(sh < 130 ? q1 >> (sh - 66) : q2 >> (sh - 130)) & 3u;
     }
-    const uint64_t tr = theta + (1ull << 55);
-    const int k = (int)(tr >> 56);
-    const long long d = (long long)(theta - (tr & ~((1ull << 56) - 1))); // [-2^55, 2^55)
+    const uint64_t tr = theta + (1ull << 51);
+    const int k = (int)(tr >> 52);
+    const long long d = (long long)(theta - (tr & ~((1ull << 52) - 1))) * 4 + g; // [-2^53, 2^53)
     const bool neg_r = d < 0;
     const uint64_t a = (uint64_t)(neg_r ? -d : d);
-    const uint64_t R = __umul64hi(a << 8, TWO_PI_Q61); // |r| 2^69
-    const uint64_t u = __umul64hi(R, R);               // r^2 2^74
-    const uint64_t H = C_H24 - __umul64hi(u, C_K720);  // (1/24 - u/720) 2^68
-    const uint64_t G = (1ull << 63) - (__umul64hi(u, H) >> 14);  // (1/2 - u (1/24 - u/720)) 2^64
-    const uint64_t cr = (1ull << 63) - (__umul64hi(u, G) >> 11); // cos r 2^63
-    const uint64_t J = C_J120 - __umul64hi(u, C_K5040);          // (1/120 - u/5040) 2^70
-    const uint64_t I = C_I6 - (__umul64hi(u, J) >> 14);          // (1/6 - u (...)) 2^66
-    const uint64_t S1 = (1ull << 63) - (__umul64hi(u, I) >> 13); // sin r / r 2^63
-    const uint64_t sr = __umul64hi(R, S1);                       // |sin r| 2^68
-    const ulonglong2 cs = quad[k & 63];
-    const bool odd = (k >> 6) & 1;
-    // quadrants 0..3: cos(phi), -sin(phi), -cos(phi), sin(phi) with phi = j pi / 128 + r
-    const long long p1 = (long long)__umul64hi(odd ? cs.y : cs.x, cr);
-    const long long p2 = (long long)(__umul64hi(odd ? cs.x : cs.y, sr) >> 5);
+    const uint64_t R = __umul64hi(a << 10, TWO_PI_Q61); // |r| 2^73
+    const uint64_t u = __umul64hi(R, R);                // r^2 2^82
+    const uint32_t u32 = (uint32_t)(u >> 31);           // r^2 2^51
+    const uint32_t r32 = (uint32_t)(R >> 31);           // |r| 2^42
+    const uint32_t hi3 = __umulhi(r32, u32);            // |r|^3 2^61
+    // 1 - cos r = r^2/2 - r^4/24 (times 2^63); p1 = A cos r = A/2 - A (1 - cos r), each a two-term
+    // difference (the fused form 2^63 - x + t came out wrong on sm_103a when x = t = 0)
+    const uint64_t dev = (u >> 20) - __umulhi(__umulhi(u32, u32), C_INV3072);
+    const uint64_t sr = R - (((uint64_t)hi3 * C_INV6) >> 20) + __umulhi(__umulhi(hi3, u32), C_INV15360); // |sin r| 2^73
+    const ulonglong2 cs = quad[k & (kQuadrant - 1)];
+    const bool odd = (k >> 10) & 1;
+    // quadrants 0..3: cos(phi), -sin(phi), -cos(phi), sin(phi) with phi = j pi / 2048 + r
+    const uint64_t A = odd ? cs.y : cs.x;
+    const long long p1 = (long long)((A >> 1) - __umul64hi(A, dev));
+    const long long p2 = (long long)((__umul64hi(odd ? cs.x : cs.y, sr) + 512) >> 10);
     const long long v = odd == neg_r ? p1 - p2 : p1 + p2;
-    out = (((k >> 6) + 1) & 2) ? -v : v;
+    out = (((k >> 10) + 1) & 2) ? -v : v;
     return true;
 }
 
@@ -165,14 +168,21 @@ __global__ void field_table_kernel(double dg, int n, double *__restrict__ btab)
 
 // WF (single phase): per-walker decrease factors; pAlive is then the walker's own running FP64
 // product, one multiply per collision, exactly the reference's `local_pAlive *= local_dFactor`.
-template <int BC, int NP, bool UNIFORM, bool WF>
-__global__ void __launch_bounds__(kWalkThreads) cpmg_field_kernel(DevImage im, WalkState st, FieldLaunch L)
+// MORTON (noflux, no voxel division, uniform field): steps on the image's Morton copy (see
+// cpmg_walk_kernel) with the coordinate along the gradient carried beside the Morton index: a move
+// changes it by one exactly when it changes the index's bits of that axis, in the direction those
+// bits moved (dilated integers keep their order).
+template <int BC, int NP, bool UNIFORM, bool WF, bool MORTON = false>
+__global__ void __launch_bounds__(kWalkThreads, MORTON ? 6 : 4) cpmg_field_kernel(DevImage im, WalkState st, FieldLaunch L)
 {
     static_assert(!WF || NP == 1, "per-walker decrease factors are for single-phase images");
+    static_assert(!MORTON || (BC == BC_NOFLUX && UNIFORM), "the Morton field walk is the noflux uniform-field walk");
     constexpr int W = WordsPerBlock<NP>::value;
     constexpr int K = 3;
     __shared__ unsigned long long sacc[32 * K];
-    __shared__ ulonglong2 quad[64];
+    __shared__ ulonglong2 quad[kQuadrant]; // 16 KB: cos / sin of the first quadrant
+    __shared__ uint4 sdir[6];              // MORTON: direction table
+    if (MORTON && threadIdx.x < 6) sdir[threadIdx.x] = morton_direction(im.mi, threadIdx.x);
 
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -218,9 +228,19 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_field_kernel(DevImage im, W
     }
     const double B0 = active ? field_at<BC, W, UNIFORM>(im, p, L, true) : 0.0;
     double B = B0;
+    uint32_t P = 0, gm = 0; // MORTON: Morton index, its bits of the gradient axis
+    int gc = 0;             // MORTON: coordinate along the gradient axis
+    if (MORTON)
+    {
+        gm = L.axis == 0 ? im.mi.mx : (L.axis == 1 ? im.mi.my : im.mi.mz);
+        gc = L.axis == 0 ? p.x : (L.axis == 1 ? p.y : p.z);
+        if (active)
+            P = dilate_bits((uint32_t)p.x, im.mi.mx) | dilate_bits((uint32_t)p.y, im.mi.my) |
+                dilate_bits((uint32_t)p.z, im.mi.mz);
+    }
 
     for (int k = threadIdx.x; k < 32 * K; k += blockDim.x) sacc[k] = 0;
-    for (int k = threadIdx.x; k < 64; k += blockDim.x)
+    for (int k = threadIdx.x; k < kQuadrant; k += blockDim.x)
         quad[k] = make_ulonglong2(kQuadrantCosSin[k][0], kQuadrantCosSin[k][1]);
     __syncthreads();
     // pAlive as 2^63 fixed point: the survival tables, or the walker's own FP64 product converted
@@ -254,13 +274,23 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_field_kernel(DevImage im, W
 #pragma unroll 1
                 for (int inv = 0; inv < 2; inv++)
                 {
-                    phase = -phase;
+                    // the inversion: an exact sign flip, on the integer pipe (FP64 is this kernel's
+                    // scarce pipe)
+                    phase = __longlong_as_double(__double_as_longlong(phase) ^ (long long)(1ull << 63));
                     for (int s = 0; s < L.steps_per_inversion; s++)
                     {
                         phase = __fma_rn(L.gammatau, B, phase);
                         bool wall;
                         int ph;
-                        walker_step<BC, W>(im, p, seed, wall, ph);
+                        if (MORTON)
+                        {
+                            const uint32_t f0 = P & gm;
+                            morton_step<W>(im.mi, sdir, P, seed, wall, ph);
+                            const uint32_t f1 = P & gm;
+                            gc += (f1 > f0 ? 1 : 0) - (f1 < f0 ? 1 : 0);
+                        }
+                        else
+                            walker_step<BC, W>(im, p, seed, wall, ph);
                         if (wall)
                         {
 #pragma unroll
@@ -269,7 +299,7 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_field_kernel(DevImage im, W
                         }
                         else
                         {
-                            B = field_at<BC, W, UNIFORM>(im, p, L, false);
+                            B = MORTON ? __ldg(L.btab + gc) : field_at<BC, W, UNIFORM>(im, p, L, false);
                         }
                         phase = __fma_rn(L.gammatau, B, phase);
                     }
@@ -303,6 +333,12 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_field_kernel(DevImage im, W
 
     if (active)
     {
+        if (MORTON)
+        {
+            p.x = (int)undilate_bits(P, im.mi.mx);
+            p.y = (int)undilate_bits(P, im.mi.my);
+            p.z = (int)undilate_bits(P, im.mi.mz);
+        }
         st.x[i] = p.x;
         st.y[i] = p.y;
         st.z[i] = p.z;
@@ -346,10 +382,26 @@ cudaError_t launch_cpmg_field(int bc_key, int np, bool uniform, const DevImage &
             {
                 if (L.wf)
                 {
+                    if constexpr (BC == BC_NOFLUX)
+                    {
+                        if (uniform && im.mi.words)
+                        {
+                            cpmg_field_kernel<BC, 1, true, true, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                            return;
+                        }
+                    }
                     if (uniform)
                         cpmg_field_kernel<BC, 1, true, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
                     else
                         cpmg_field_kernel<BC, 1, false, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    return;
+                }
+            }
+            if constexpr (BC == BC_NOFLUX)
+            {
+                if (uniform && im.mi.words)
+                {
+                    cpmg_field_kernel<BC, NP, true, false, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
                     return;
                 }
             }

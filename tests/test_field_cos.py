@@ -18,11 +18,16 @@ import cos_table  # noqa: E402
 
 C = cos_table.constants()
 M64 = (1 << 64) - 1
-BOUND_Q62 = 4  # |cos_q62(x) - cos(x) * 2^62| < 4
+M32 = (1 << 32) - 1
+BOUND_Q62 = 2.5  # |cos_q62(x) - cos(x) * 2^62| < 2.5
 
 
 def umulhi(a, b):
     return (a * b) >> 64
+
+
+def umulhi32(a, b):
+    return (a * b) >> 32
 
 
 def cos_q62(phase):
@@ -32,34 +37,33 @@ def cos_q62(phase):
     if ex >= 1063:
         return None
     sh = 1139 - ex
-    theta = 0
+    theta = g = 0
     if ex != 0 and sh < 178:
         m = (bits & ((1 << 52) - 1)) | (1 << 52)
         lo2 = (m * C["INV_2PI_HI"]) & M64
         q1 = (umulhi(m, C["INV_2PI_LO"]) + lo2) & M64
         q2 = (umulhi(m, C["INV_2PI_HI"]) + (1 if q1 < lo2 else 0)) & M64
         theta = ((q1 >> (sh - 64)) | (q2 << (128 - sh))) & M64 if sh < 128 else q2 >> (sh - 128)
-    tr = (theta + (1 << 55)) & M64
-    k = tr >> 56
-    d = (theta - (tr & ~((1 << 56) - 1))) & M64
-    d = d - (1 << 64) if d >> 63 else d
+        g = ((q1 >> (sh - 66)) if sh < 130 else (q2 >> (sh - 130))) & 3
+    tr = (theta + (1 << 51)) & M64
+    k = tr >> 52
+    d = (theta - (tr & ~((1 << 52) - 1))) & M64
+    d = (d - (1 << 64) if d >> 63 else d) * 4 + g
     neg_r = d < 0
     a = -d if neg_r else d
-    R = umulhi((a << 8) & M64, C["TWO_PI_Q61"])
+    R = umulhi((a << 10) & M64, C["TWO_PI_Q61"])
     u = umulhi(R, R)
-    H = C["C_H24"] - umulhi(u, C["C_K720"])
-    G = (1 << 63) - (umulhi(u, H) >> 14)
-    cr = (1 << 63) - (umulhi(u, G) >> 11)
-    J = C["C_J120"] - umulhi(u, C["C_K5040"])
-    I = C["C_I6"] - (umulhi(u, J) >> 14)
-    S1 = (1 << 63) - (umulhi(u, I) >> 13)
-    sr = umulhi(R, S1)
-    cj, sj = C["table"][k & 63]
-    odd = (k >> 6) & 1
-    p1 = umulhi(sj if odd else cj, cr)
-    p2 = umulhi(cj if odd else sj, sr) >> 5
+    u32, r32 = (u >> 31) & M32, (R >> 31) & M32
+    hi3 = umulhi32(r32, u32)
+    dev = (u >> 20) - umulhi32(umulhi32(u32, u32), C["C_INV3072"])
+    sr = R - ((hi3 * C["C_INV6"]) >> 20) + umulhi32(umulhi32(hi3, u32), C["C_INV15360"])
+    cj, sj = C["table"][k & (cos_table.QUADRANT - 1)]
+    odd = (k >> 10) & 1
+    A = sj if odd else cj
+    p1 = (A >> 1) - umulhi(A, dev)
+    p2 = (umulhi(cj if odd else sj, sr) + 512) >> 10
     v = p1 - p2 if bool(odd) == neg_r else p1 + p2
-    return -v if ((k >> 6) + 1) & 2 else v
+    return -v if ((k >> 10) + 1) & 2 else v
 
 
 def prob_q63(p):
@@ -98,8 +102,9 @@ def test_generator_constants():
     assert abs(C["TWO_PI_Q61"] / 2.0 ** 61 - 2 * math.pi) < 1e-15
     assert abs(((C["INV_2PI_HI"] << 64) | C["INV_2PI_LO"]) / 2.0 ** 128 - 1 / (2 * math.pi)) < 1e-17
     for j, (cv, sv) in enumerate(C["table"]):
-        assert abs(cv / 2.0 ** 63 - math.cos(j * math.pi / 128)) < 1e-15
-        assert abs(sv / 2.0 ** 63 - math.sin(j * math.pi / 128)) < 1e-15
+        assert abs(cv / 2.0 ** 63 - math.cos(j * math.pi / 2048)) < 1e-15
+        assert abs(sv / 2.0 ** 63 - math.sin(j * math.pi / 2048)) < 1e-15
+    assert len(C["table"]) == cos_table.QUADRANT == 1024
     assert C["table"][0] == (1 << 63, 0)
 
 
@@ -116,13 +121,13 @@ def phases(n, seed):
         elif r < 0.8:
             out.append(rng.uniform(-1e11, 1e11))
         else:  # at the table's and the quadrants' boundaries
-            out.append(rng.randint(-40000, 40000) * math.pi / 256 + rng.uniform(-1e-12, 1e-12))
+            out.append(rng.randint(-400000, 400000) * math.pi / 2048 + rng.uniform(-1e-12, 1e-12))
     return out
 
 
 def test_fixed_point_cosine_error_bound():
     worst = Fraction(0)
-    for x in phases(4000, 11):
+    for x in phases(6000, 11):
         err = abs(cos_q62(x) - exact_cos_q62(x))
         worst = max(worst, err)
     assert worst < BOUND_Q62, float(worst)

@@ -183,11 +183,13 @@ def _fp64_powers(f, n):
     return out
 
 
+@pytest.mark.parametrize("bc", ["noflux", "periodic"])
 @pytest.mark.parametrize("case", ["one_phase", "two_phases", "per_walker"])
-def test_field_energies_within_fixed_point_bound(engine, oracle, case):
+def test_field_energies_within_fixed_point_bound(engine, oracle, case, bc):
     """The kernel's exact echo sums against exact values: every walker's E * 2^61 (pAlive from its
     collision counts, cos from its final phase, both downloaded) within 3 units of pAlive * cos(phase)
-    * 2^61 computed with a 256-bit cosine, so the last echo's integer sum is within 3 n units."""
+    * 2^61 computed with a 256-bit cosine, so the last echo's integer sum is within 3 n units. Both
+    kernel families: the noflux walk on the Morton copy and the bit-block walk (periodic)."""
     n_phases = 2 if case == "two_phases" else 1
     lab = image(seed=21, n_phases=n_phases)
     w = walkers(lab, 900, 8)
@@ -199,10 +201,11 @@ def test_field_energies_within_fixed_point_bound(engine, oracle, case):
     if case == "per_walker":
         f = dfactor(np.random.default_rng(5).uniform(2.0, 60.0, n))
         engine.set_walker_dfactor(f)
-        g = engine.cpmg_field(30, 4, None, GAMMA, TIME_INTERVAL)
+        g = engine.cpmg_field(30, 4, None, GAMMA, TIME_INTERVAL, bc=bc)
     else:
-        g = engine.cpmg_field(30, 4, dfactor(rho), GAMMA, TIME_INTERVAL)
+        g = engine.cpmg_field(30, 4, dfactor(rho), GAMMA, TIME_INTERVAL, bc=bc)
     st = engine.download_walkers()
+    assert engine.morton_layout
     assert g["echo_fx"][0] == n << 62  # phase 0, pAlive 1: every walker adds 2^61 + 2^61
     assert np.ptp(g["phase"]) > 10.0
     coll = st["collisions"]
@@ -220,3 +223,29 @@ def test_field_energies_within_fixed_point_bound(engine, oracle, case):
             exact += pal * exact_cos_q62(float(g["phase"][k])) / 2
     err = abs(Fraction(g["echo_fx"][-1] - (n << 61)) - exact)
     assert err < 3 * n, float(err / n)
+
+
+@pytest.mark.parametrize("n_phases", [1, 2])
+def test_field_walk_layouts_identical(engine, n_phases):
+    """The uniform-field noflux walk on the image's Morton copy (gradient coordinate carried beside the
+    Morton index) and on the bit blocks: positions, seeds, collisions, phases and exact sums equal,
+    along every gradient axis."""
+    lab = image(shape=(37, 22, 30), seed=9, n_phases=n_phases)
+    w = walkers(lab, 2500, 13)
+    rho = [8.0, 30.0][:n_phases]
+    for axis in range(3):
+        outs = []
+        for morton in (True, False):
+            engine.allow_morton(morton)
+            engine.upload_labels(lab, n_phases)
+            assert engine.morton_layout == morton
+            engine.upload_walkers(*w)
+            engine.set_field_uniform(15.0, axis, RES)
+            g = engine.cpmg_field(40, 4, dfactor(rho), GAMMA, TIME_INTERVAL, echoes_per_launch=32)
+            outs.append((g, engine.download_walkers()))
+        (a, sa), (b, sb) = outs
+        assert a["echo_fx"] == b["echo_fx"]
+        assert np.array_equal(a["phase"].view(np.uint64), b["phase"].view(np.uint64))
+        for key in ("x", "y", "z", "seed", "collisions"):
+            assert np.array_equal(sa[key], sb[key])
+    engine.allow_morton(True)
