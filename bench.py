@@ -218,7 +218,8 @@ def _sphere_image(args):
 
 def run_fit_multiphase(args):
     """Differentiable CPMG fit of a multi-phase image: 200^3, 4 solid phases, 500k walkers, 5000 echoes
-    of 3 steps; L-BFGS with adjoint gradients vs the restated GA (population 64) on the same GPU walk."""
+    of 3 steps; L-BFGS with gradients from the walk's forward sensitivities (one walk per evaluation) vs the
+    restated GA (population 64) on the same GPU walk."""
     import torch
 
     from randomwalk_nmr_gb300 import Engine

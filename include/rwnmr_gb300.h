@@ -128,6 +128,19 @@ typedef struct rwnmr_cpmg_params
 rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, double *echo_sum, uint64_t *echo_fx,
                             uint64_t *echo_coll);
 
+/* rwnmr_cpmg_run (same walk, same echo_sum) that also returns the forward sensitivities of the echo
+ * sums to the per-phase decrease factors, for gradients without a second walk:
+ *   echo_sens    [(n_echoes+1)*n_phases] sum over walkers of E_w(e) * c_wq(e), the walker's energy
+ *                after echo e times its collisions with phase q so far, so that
+ *                d echo_sum[e] / d dfactor[q] = echo_sens[e][q] / dfactor[q] for dfactor[q] > 0
+ *   echo_sens_fx [(n_echoes+1)*n_phases*4] the same sums exactly: each walker's product of its 2^-63
+ *                fixed-point energy and its count (96 bits) split into bits 0-23, 24-47, 48-71,
+ *                72-95, each limb summed over walkers
+ * Both nullable. Per-phase decrease factors only (dfactor must not be NULL). No counterpart in the
+ * reference. */
+rwnmr_status rwnmr_cpmg_run_sens(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, double *echo_sum, double *echo_sens,
+                                 uint64_t *echo_sens_fx);
+
 /* Vector-Jacobian product of rwnmr_cpmg_run by replaying every trajectory from its stored seed:
  * grad_dfactor[p] = sum_e grad_echo[e] * d echo_sum[e] / d dfactor[p]. grad_echo: [n_echoes+1]. */
 rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, const double *grad_echo,

@@ -2,10 +2,13 @@
 
 * :func:`cpmg_decay` -- the CPMG echo train ``M(t_e) = exp(-t_e/T2b) * sum_w E_w(e) / N`` as a
   differentiable function of the surface relaxivity of each material phase and of the bulk T2.
-  Forward is one GPU walk (``rwnmr_cpmg_run``); backward is the seed-replay adjoint kernel
-  (``rwnmr_cpmg_adjoint``), which replays every trajectory from its stored RNG seed instead of
-  storing per-step checkpoints. For fixed trajectories the echo train is smooth in rho and T2b,
-  which is what these derivatives are (pathwise derivatives under common random numbers).
+  Forward is one GPU walk. When rho needs a gradient and every decrease factor is positive, that
+  walk also sums the forward sensitivities sum_w E_w(e) c_wq(e) exactly (``rwnmr_cpmg_run_sens``)
+  and backward is host arithmetic, d echo_sum / d f_q = sens_q / f_q; otherwise forward is
+  ``rwnmr_cpmg_run`` and backward the seed-replay adjoint kernel (``rwnmr_cpmg_adjoint``), which
+  replays every trajectory from its stored RNG seed. For fixed trajectories the echo train is
+  smooth in rho and T2b, which is what these derivatives are (pathwise derivatives under common
+  random numbers).
 * :func:`pfgse_attenuation` -- PFGSE attenuation ``M(g_j, Delta)/M(0, Delta)`` as a function of the
   gradient strengths g_j along a fixed direction, backward through ``rwnmr_pfgse_grad_g``.
 
@@ -37,7 +40,12 @@ class _CpmgDecay(torch.autograd.Function):
         rho_np = rho.detach().cpu().double().numpy().reshape(-1)
         dfdrho = -(2.0 / 3.0) * res / (d0 * 1e3)
         f = 1.0 + dfdrho * rho_np
-        raw = engine.cpmg(n_echoes, steps_per_echo, f, bc=bc, shift=shift)["echo_sum"]
+        ctx.sens = None
+        if ctx.needs_input_grad[0] and np.all(f > 0.0):
+            out = engine.cpmg_sens(n_echoes, steps_per_echo, f, bc=bc, shift=shift)
+            raw, ctx.sens = out["echo_sum"], out["sens"]
+        else:
+            raw = engine.cpmg(n_echoes, steps_per_echo, f, bc=bc, shift=shift)["echo_sum"]
         dt = res * res / (6.0 * d0)
         t = echo_times(n_echoes, steps_per_echo, dt)
         T2 = float(t2b.detach().cpu())
@@ -59,7 +67,10 @@ class _CpmgDecay(torch.autograd.Function):
         grad_rho = grad_t2 = None
         if ctx.needs_input_grad[0]:
             g_raw = g * bulk.numpy() / n0
-            gf = ctx.engine.cpmg_adjoint(n_echoes, spe, f, g_raw, bc=bc, shift=shift)
+            if ctx.sens is not None:
+                gf = (g_raw @ ctx.sens) / f  # no walk: the forward sensitivities
+            else:
+                gf = ctx.engine.cpmg_adjoint(n_echoes, spe, f, g_raw, bc=bc, shift=shift)
             dt_, dev, shape = ctx.rho_meta
             grad_rho = torch.from_numpy(gf * dfdrho).to(dtype=dt_, device=dev).reshape(shape)
         if ctx.needs_input_grad[1]:

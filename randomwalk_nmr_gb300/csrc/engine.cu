@@ -549,12 +549,16 @@ rwnmr_status rwnmr_walkers_set_dfactor(rwnmr_ctx *c, const double *dfactor)
 }
 
 // ---- CPMG -------------------------------------------------------------------------------------
-rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *echo_sum, uint64_t *echo_fx,
-                            uint64_t *echo_coll)
+namespace
+{
+// rwnmr_cpmg_run, and with sens the sensitivity sums of rwnmr_cpmg_run_sens
+rwnmr_status cpmg_impl(rwnmr_ctx *c, const rwnmr_cpmg_params *p, bool sens, double *echo_sum, uint64_t *echo_fx,
+                       uint64_t *echo_coll, double *echo_sens, uint64_t *echo_sens_fx)
 {
     RW_TRY(need_run_state(c));
     if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
     RW_TRY(check_geom(c, p->bc, p->shift));
+    if (sens && !p->dfactor) return c->fail(RWNMR_ERR_UNSUPPORTED, "sensitivities are for per-phase decrease factors");
     const bool per_walker = p->dfactor == nullptr;
     RW_TRY(per_walker ? check_walker_dfactor(c) : check_dfactor(c, p->dfactor));
     if (p->n_echoes < 0 || p->steps_per_echo < 1) return c->fail(RWNMR_ERR_INVALID, "bad echo count / steps per echo");
@@ -562,7 +566,7 @@ rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *ec
     if (nmax > (1ll << 28)) return c->fail(RWNMR_ERR_UNSUPPORTED, "walk of %lld steps too long", (long long)nmax);
     cudaSetDevice(c->device);
     const int slots = phase_slots(c->n_phases);
-    const int K = 3 + slots;
+    const int K = 3 + slots + (sens ? 4 * slots : 0);
     if (per_walker)
         RW_CUDA(c, c->wenergy.ensure((size_t)std::max<int64_t>(c->n, 1)), "walker energies");
     else
@@ -582,6 +586,7 @@ rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *ec
     CpmgLaunch L{};
     L.steps_per_echo = p->steps_per_echo;
     L.record = 1;
+    L.sens = sens ? 1 : 0;
     L.tfx = per_walker ? nullptr : c->tfx.p;
     L.tstride = (int)(nmax + 1);
     L.wf = per_walker ? c->wf.p : nullptr;
@@ -623,8 +628,33 @@ rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *ec
             for (int k = 0; k < 3; k++) echo_fx[(size_t)e * 3 + k] = a[k];
         if (echo_coll && e > 0)
             for (int q = 0; q < c->n_phases; q++) echo_coll[(size_t)(e - 1) * c->n_phases + q] = a[3 + q];
+        if (sens)
+            for (int q = 0; q < c->n_phases; q++)
+            {
+                const unsigned long long *l = a + 3 + slots + 4 * q; // 24-bit limbs of sum E c_q
+                if (echo_sens_fx)
+                    for (int k = 0; k < 4; k++) echo_sens_fx[((size_t)e * c->n_phases + q) * 4 + k] = l[k];
+                if (echo_sens)
+                {
+                    const u128 v = (u128)l[0] + ((u128)l[1] << 24) + ((u128)l[2] << 48) + ((u128)l[3] << 72);
+                    echo_sens[(size_t)e * c->n_phases + q] = std::ldexp((double)v, -63);
+                }
+            }
     }
     return RWNMR_OK;
+}
+} // namespace
+
+rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *echo_sum, uint64_t *echo_fx,
+                            uint64_t *echo_coll)
+{
+    return cpmg_impl(c, p, false, echo_sum, echo_fx, echo_coll, nullptr, nullptr);
+}
+
+rwnmr_status rwnmr_cpmg_run_sens(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *echo_sum, double *echo_sens,
+                                 uint64_t *echo_sens_fx)
+{
+    return cpmg_impl(c, p, true, echo_sum, nullptr, nullptr, echo_sens, echo_sens_fx);
 }
 
 // ---- internal field ---------------------------------------------------------------------------

@@ -56,9 +56,10 @@ __device__ __forceinline__ void load_pos(const WalkState &s, int64_t i, WalkerPo
 // Occupancy: at 256 threads, 8 resident blocks per SM need <= 32 registers a thread, 6 need <= 40,
 // 5 need <= 48. The minimum-block bounds below were chosen by measurement (+4 % two-phase, +6 %
 // one-phase walker-steps/s over the unbounded build); a few instances spill up to 16 bytes.
-template <int BC, int NP, bool PACK, bool WF>
+template <int BC, int NP, bool PACK, bool WF, bool SENS = false>
 constexpr int cpmg_min_blocks()
 {
+    if (SENS) return NP == 4 ? 5 : 6; // the sensitivity sums need more than 32 registers
     return NP == 4 ? 5 : ((BC == BC_NOFLUX || BC == BC_GENERIC) && !WF && (NP == 1 || PACK) ? 8 : 6);
 }
 
@@ -66,18 +67,23 @@ constexpr int cpmg_min_blocks()
 // so the step loop unrolls away.
 // MORTON (noflux, no voxel division): the walk runs on the image's Morton copy with the position held
 // as one Morton index (morton_step), converted from and back to x, y, z once per launch.
-template <int BC, int NP, bool PACK, bool WF, int SPE, bool MORTON = false>
-__global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, WF>()))
+// SENS (per-phase tables): after each echo also the exact sums over walkers of E * c_q, the walker's
+// 2^-63 fixed-point energy times its collision count with phase q -- the forward sensitivities,
+// d(echo sum)/d f_q = sum E c_q / f_q. Each 96-bit product is summed as four 24-bit limbs.
+template <int BC, int NP, bool PACK, bool WF, int SPE, bool MORTON = false, bool SENS = false>
+__global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, WF, SENS>()))
     cpmg_walk_kernel(DevImage im, WalkState st, CpmgLaunch L)
 {
     static_assert(!PACK || NP == 2, "packed collision counts are for two phases");
     static_assert(!WF || NP == 1, "per-walker decrease factors are for single-phase images");
     static_assert(!MORTON || BC == BC_NOFLUX, "the Morton walk is the noflux walk");
+    static_assert(!SENS || (!PACK && !WF), "sensitivities use unpacked counts and the per-phase tables");
     constexpr int W = WordsPerBlock<NP>::value;
-    constexpr int NG = PACK ? 1 : NP; // collision-count words per echo
-    constexpr int KK = 3 + NG;        // values kept per echo
-    constexpr int K = 3 + NP;         // values per echo in the accumulators
-    constexpr int KP = KK <= 4 ? 4 : 8; // KK padded to whole 16-byte stores
+    constexpr int NG = PACK ? 1 : NP;    // collision-count words per echo
+    constexpr int KS = SENS ? 4 * NP : 0; // SENS: limbs of sum E c_q per echo
+    constexpr int KK = 3 + NG + KS;       // values kept per echo
+    constexpr int K = 3 + NP + KS;        // values per echo in the accumulators
+    constexpr int KP = (KK + 3) / 4 * 4;  // KK padded to whole 16-byte stores
     // each warp's sums of the current 32-echo window, [warp][echo][value]: lane 0 stores them after
     // the reductions, the CTA adds the warps up when the window is flushed
     __shared__ __align__(16) uint32_t wsum[kWalkThreads / 32][32][KP];
@@ -209,8 +215,23 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                 r[2] = __reduce_add_sync(FULL, (uint32_t)(efx >> 42));
 #pragma unroll
                 for (int k = 0; k < NG; k++) r[3 + k] = __reduce_add_sync(FULL, g[k]);
+                if (SENS)
+                {
+                    constexpr uint32_t M24 = (1u << 24) - 1;
 #pragma unroll
-                for (int k = 3 + NG; k < KP; k++) r[k] = 0;
+                    for (int q = 0; q < NP; q++)
+                    {
+                        const uint64_t lo = efx * (uint64_t)c[q];                     // bits 0-63 of E c_q
+                        const uint32_t hi = (uint32_t)__umul64hi(efx, (uint64_t)c[q]); // bits 64-95
+                        uint32_t *rq = r + 3 + NG + 4 * q;
+                        rq[0] = __reduce_add_sync(FULL, (uint32_t)lo & M24);
+                        rq[1] = __reduce_add_sync(FULL, (uint32_t)(lo >> 24) & M24);
+                        rq[2] = __reduce_add_sync(FULL, ((uint32_t)(lo >> 48) | (hi << 16)) & M24);
+                        rq[3] = __reduce_add_sync(FULL, hi >> 8);
+                    }
+                }
+#pragma unroll
+                for (int k = 3 + NG + KS; k < KP; k++) r[k] = 0;
                 if (lane == 0)
                 {
                     uint4 *slot = reinterpret_cast<uint4 *>(&wsum[threadIdx.x >> 5][e - e0][0]);
@@ -702,6 +723,15 @@ cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkS
             auto run_m = [&](auto spe, auto mort) {
                 constexpr int SPE = decltype(spe)::value;
                 constexpr bool M = decltype(mort)::value;
+                if (L.sens)
+                {
+                    // sensitivity walks: the Morton instance, or the runtime-bc instance for the rest
+                    if constexpr (M)
+                        cpmg_walk_kernel<BC, NP, false, false, SPE, true, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    else
+                        cpmg_walk_kernel<BC_GENERIC, NP, false, false, 0, false, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                    return;
+                }
                 if constexpr (NP == 1)
                 {
                     if (L.wf)

@@ -36,11 +36,12 @@ struct CpmgLaunch
     int steps_per_echo;
     int from_initial;      // 1: start from (x0, seed0) with zero collisions; 0: continue (x, seed, coll)
     int record;            // accumulate per-echo sums into acc
+    int sens;              // with record and the tables: also the sensitivity sums sum E c_q (4 limbs per phase)
     const uint64_t *tfx;   // [n_phases][tstride] fixed-point energy tables
     int tstride;
     const double *wf;      // per-walker decrease factors [n] (single phase), or null for the tables
     double *wenergy;       // per-walker FP64 energies [n], carried across launches (with wf)
-    unsigned long long *acc; // [(n_echoes+1)][3 + NP]
+    unsigned long long *acc; // [(n_echoes+1)][3 + NP (+ 4 NP with sens)]
     unsigned *status;
 };
 

@@ -34,7 +34,7 @@ EXPORTS = [
     "rwnmr_ctx_create", "rwnmr_ctx_destroy", "rwnmr_last_error", "rwnmr_version", "rwnmr_ctx_set_stream",
     "rwnmr_ctx_launch_count", "rwnmr_ctx_last_kernel_ms", "rwnmr_image_upload", "rwnmr_image_upload_labels",
     "rwnmr_image_download_blocks", "rwnmr_image_layout", "rwnmr_ctx_set_image_layout", "rwnmr_walkers_upload", "rwnmr_walkers_download", "rwnmr_cpmg_run",
-    "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_map_continue", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
+    "rwnmr_cpmg_run_sens", "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_map_continue", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
     "rwnmr_cpmg_run_noalloc", "rwnmr_batch_create", "rwnmr_batch_destroy", "rwnmr_batch_last_error",
     "rwnmr_batch_last_kernel_ms", "rwnmr_batch_launch_count", "rwnmr_batch_add_image", "rwnmr_batch_cpmg",
     "rwnmr_batch_autotune", "rwnmr_batch_collision_histogram", "rwnmr_batch_histogram_walk_ms",
@@ -238,6 +238,22 @@ class Engine:
         echo_coll = np.zeros((n_echoes, self.n_phases), np.uint64)
         self._check(self.lib.rwnmr_cpmg_run(self.ctx, ctypes.byref(prm), _p(echo_sum), _p(echo_fx), _p(echo_coll)))
         return dict(echo_sum=echo_sum, echo_fx=echo_fx, echo_coll=echo_coll)
+
+    def cpmg_sens(self, n_echoes: int, steps_per_echo: int, dfactor, bc: str = "noflux", shift: int = 0,
+                  echoes_per_launch: int = 0):
+        """The CPMG walk with forward sensitivities: echo_sum as cpmg(), sens [n_echoes+1][n_phases] =
+        sum over walkers of E * c_q (d echo_sum / d dfactor_q = sens / dfactor_q), and sens_fx, the same
+        sums as exact Python ints in units of 2^-63."""
+        df = self._dfactor(dfactor)
+        if df is None:
+            raise ValueError("sensitivities are for per-phase decrease factors")
+        prm = CpmgParams(BC[bc], int(shift), int(steps_per_echo), int(n_echoes), _dptr(df), int(echoes_per_launch))
+        echo_sum = np.zeros(n_echoes + 1)
+        sens = np.zeros((n_echoes + 1, self.n_phases))
+        limbs = np.zeros((n_echoes + 1, self.n_phases, 4), np.uint64)
+        self._check(self.lib.rwnmr_cpmg_run_sens(self.ctx, ctypes.byref(prm), _p(echo_sum), _p(sens), _p(limbs)))
+        sens_fx = [[sum(int(v) << (24 * k) for k, v in enumerate(row)) for row in e] for e in limbs]
+        return dict(echo_sum=echo_sum, sens=sens, sens_fx=sens_fx)
 
     def cpmg_adjoint(self, n_echoes: int, steps_per_echo: int, dfactor, grad_echo, bc: str = "noflux",
                      shift: int = 0):

@@ -5,7 +5,9 @@
   returns every candidate's echo train and its exact derivative, and each candidate takes a
   Gauss-Newton step on its own least-squares misfit. The best candidate per image wins.
 * :func:`fit_rho_adjoint` -- one image with several material phases: L-BFGS on the relaxivity
-  vector with gradients from the seed-replay adjoint (``cpmg_decay`` / ``rwnmr_cpmg_adjoint``).
+  vector through ``cpmg_decay``, one walk per evaluation: the walk returns the echo train and its
+  exact forward sensitivities (``rwnmr_cpmg_run_sens``), so the gradient needs no second walk (the
+  seed-replay adjoint ``rwnmr_cpmg_adjoint`` covers a zero decrease factor).
 
 Both report the GPU time they spent (sum of the walk kernels' device time).
 """
@@ -62,7 +64,8 @@ def fit_rho_batch(batch, targets, n_walkers, n_echoes, steps_per_echo, t2b, rho_
 def fit_rho_adjoint(engine, target, rho0, n_echoes, steps_per_echo, t2b, res=1.0, d0=2.5, max_evals=40,
                     bounds=(0.5, 100.0)):
     """L-BFGS fit of a relaxivity vector (one per material phase) to a normalised echo train,
-    gradients by the seed-replay adjoint. Returns a dict with rho, loss and GPU seconds."""
+    gradients from the walk's forward sensitivities (or the seed-replay adjoint for a zero decrease
+    factor). Returns a dict with rho, loss, GPU seconds and the number of walks."""
     tgt = torch.as_tensor(np.asarray(target, np.float64))
     scale = float(tgt.abs().max())
     # optimise in a bounded reparametrisation rho = lo + (hi - lo) * sigmoid(u)
@@ -72,16 +75,20 @@ def fit_rho_adjoint(engine, target, rho0, n_echoes, steps_per_echo, t2b, res=1.0
     t2 = torch.tensor(float(t2b), dtype=torch.float64)
     opt = torch.optim.LBFGS([u], lr=1.0, max_iter=max_evals, max_eval=max_evals, tolerance_grad=1e-12,
                             tolerance_change=1e-15, history_size=10, line_search_fn="strong_wolfe")
-    stats = dict(gpu_seconds=0.0, evals=0)
+    stats = dict(gpu_seconds=0.0, evals=0, walks=0)
 
     def closure():
         opt.zero_grad()
         rho = lo + (hi - lo) * torch.sigmoid(u)
         M = cpmg_decay(rho, t2, engine, n_echoes, steps_per_echo, res, d0)
         stats["gpu_seconds"] += engine.last_kernel_ms * 1e-3
+        stats["walks"] += 1
         loss = torch.sum(((M - tgt) / scale) ** 2)
+        launches = engine.launch_count
         loss.backward()
-        stats["gpu_seconds"] += engine.last_kernel_ms * 1e-3  # adjoint walk
+        if engine.launch_count != launches:  # an adjoint walk (the sensitivities need none)
+            stats["gpu_seconds"] += engine.last_kernel_ms * 1e-3
+            stats["walks"] += 1
         stats["evals"] += 1
         return loss
 
@@ -93,4 +100,4 @@ def fit_rho_adjoint(engine, target, rho0, n_echoes, steps_per_echo, t2b, res=1.0
         stats["gpu_seconds"] += engine.last_kernel_ms * 1e-3
         loss = float(torch.sum(((M - tgt) / scale) ** 2))
     return dict(rho=rho, loss=loss, gpu_seconds=stats["gpu_seconds"], evals=stats["evals"],
-                walks=2 * stats["evals"] + 1, wall_seconds=time.perf_counter() - t0)
+                walks=stats["walks"] + 1, wall_seconds=time.perf_counter() - t0)

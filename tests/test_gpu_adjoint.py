@@ -84,3 +84,65 @@ def test_adjoint_with_a_zero_decrease_factor(engine, oracle, f):
     g2 = engine.cpmg_adjoint(n_echoes, spe, np.array([v if v > 0 else 0.5 for v in f]), grad)
     ref2 = pathwise_gradient(oracle, lab, w, n_echoes, spe, [v if v > 0 else 0.5 for v in f], grad, n_phases)
     np.testing.assert_allclose(g2, ref2, rtol=1e-10, atol=1e-12 * np.max(np.abs(ref2)))
+
+
+def _tables_fx(f, kmax):
+    """round(f^k * 2^63), f^k the FP64 repeated product: the engine's fixed-point survival tables."""
+    from fractions import Fraction
+    out, v = [], 1.0
+    for _ in range(kmax + 1):
+        out.append(round(Fraction(v) * 2 ** 63))
+        v = v * f
+    return out
+
+
+def _fx_mul(a, b):
+    return b if a >> 63 else ((a << 1) * b) >> 64
+
+
+def _collision_histories(oracle, lab, w, n_echoes, spe, f, n_phases, bc):
+    """Per-walker collision counts after every echo [n_echoes+1][n][phases], from the oracle."""
+    counts = np.zeros((n_echoes + 1, len(w[0]), n_phases), np.int64)
+    state = [np.array(a) for a in w]
+    for e in range(n_echoes):
+        o = oracle.cpmg(lab, tuple(state), 1, spe, f, n_phases=n_phases, bc=bc, threads=4)
+        counts[e + 1] = counts[e] + o["collf"].astype(np.int64)
+        state = [o["xf"], o["yf"], o["zf"], o["seedf"]]
+    return counts
+
+
+@pytest.mark.parametrize("n_phases,morton,bc", [(1, True, "noflux"), (2, True, "noflux"), (4, True, "noflux"),
+                                                (2, False, "noflux"), (3, False, "periodic"), (1, False, "mirror")])
+def test_sensitivities_exact(engine, oracle, n_phases, morton, bc):
+    """rwnmr_cpmg_run_sens: the same echo train as rwnmr_cpmg_run, and per-echo sums of E * c_q that
+    equal, exactly, the sums formed from the oracle's per-walker collision histories and the engine's
+    fixed-point tables; their gradient equals the seed-replay adjoint's."""
+    lab, w = setup(engine, n_phases, n=1500, morton=morton)
+    assert engine.morton_layout == morton
+    n_echoes, spe = 40, 3
+    f = dfactor([10.0, 30.0, 5.0, 60.0][:n_phases])
+    out = engine.cpmg_sens(n_echoes, spe, f, bc=bc, echoes_per_launch=32)
+    plain = engine.cpmg(n_echoes, spe, f, bc=bc)
+    assert np.array_equal(out["echo_sum"], plain["echo_sum"])
+    counts = _collision_histories(oracle, lab, w, n_echoes, spe, f, n_phases, bc)
+    tabs = [_tables_fx(f[q], int(counts[..., q].max())) for q in range(n_phases)]
+    for e in range(n_echoes + 1):
+        ce = counts[e]
+        efx = []
+        for k in range(len(ce)):
+            v = tabs[0][ce[k, 0]]
+            for q in range(1, n_phases):
+                v = _fx_mul(v, tabs[q][ce[k, q]])
+            efx.append(v)
+        for q in range(n_phases):
+            assert out["sens_fx"][e][q] == sum(v * int(c) for v, c in zip(efx, ce[:, q])), (e, q)
+    rng = np.random.default_rng(1)
+    grad = rng.normal(size=n_echoes + 1)
+    np.testing.assert_allclose(grad @ out["sens"] / f, engine.cpmg_adjoint(n_echoes, spe, f, grad, bc=bc), rtol=1e-11)
+
+
+def test_sensitivities_need_per_phase_factors(engine):
+    setup(engine, 1, n=200)
+    engine.set_walker_dfactor(np.full(engine.n, 0.99))
+    with pytest.raises(Exception, match="per-phase decrease factors"):
+        engine.cpmg_sens(5, 2, None)

@@ -29,7 +29,9 @@ def test_cpmg_decay_gradients(n_phases):
     M = cpmg_decay(rho, t2b, eng, 80, 2)
     assert abs(float(M[0].detach()) - 1.0) < 1e-15
     loss = (w * M).sum()
+    launches = eng.launch_count
     loss.backward()
+    assert eng.launch_count == launches  # the forward walk's sensitivities: no second walk
 
     def L(r, T):
         with torch.no_grad():
