@@ -142,7 +142,10 @@ rwnmr_status rwnmr_cpmg_run_sens(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, dou
                                  uint64_t *echo_sens_fx);
 
 /* Vector-Jacobian product of rwnmr_cpmg_run by replaying every trajectory from its stored seed:
- * grad_dfactor[p] = sum_e grad_echo[e] * d echo_sum[e] / d dfactor[p]. grad_echo: [n_echoes+1]. */
+ * grad_dfactor[p] = sum_e grad_echo[e] * d echo_sum[e] / d dfactor[p]. grad_echo: [n_echoes+1].
+ * With every decrease factor positive the replay is one integer walk with the sensitivity sums of
+ * rwnmr_cpmg_run_sens (on scratch state); with a zero factor, an FP64 replay of the direct
+ * derivative. Either way the context's walkers are left as they were. */
 rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *ctx, const rwnmr_cpmg_params *p, const double *grad_echo,
                                 double *grad_dfactor);
 

@@ -102,6 +102,9 @@ struct rwnmr_ctx
     DevBuf<int32_t> x0, y0, z0, x, y, z;
     DevBuf<uint64_t> seed0, seed;
     DevBuf<uint32_t> coll;
+    DevBuf<int32_t> rx, ry, rz; // scratch walker state of the adjoint's sensitivity walk
+    DevBuf<uint64_t> rseed;
+    DevBuf<uint32_t> rcoll;
 
     DevBuf<uint64_t> tfx;
     DevBuf<double> tfp;
@@ -282,6 +285,7 @@ void rwnmr_ctx_destroy(rwnmr_ctx *c)
     c->grad.release(); c->partial.release(); c->partial_g.release(); c->kbuf.release(); c->Mbuf.release();
     c->gbuf.release(); c->ibuf.release(); c->disp.release(); c->energy.release();
     c->wf.release(); c->wenergy.release(); c->field.release(); c->phase.release(); c->btab.release();
+    c->rx.release(); c->ry.release(); c->rz.release(); c->rseed.release(); c->rcoll.release();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -551,9 +555,10 @@ rwnmr_status rwnmr_walkers_set_dfactor(rwnmr_ctx *c, const double *dfactor)
 // ---- CPMG -------------------------------------------------------------------------------------
 namespace
 {
-// rwnmr_cpmg_run, and with sens the sensitivity sums of rwnmr_cpmg_run_sens
-rwnmr_status cpmg_impl(rwnmr_ctx *c, const rwnmr_cpmg_params *p, bool sens, double *echo_sum, uint64_t *echo_fx,
-                       uint64_t *echo_coll, double *echo_sens, uint64_t *echo_sens_fx)
+// rwnmr_cpmg_run, and with sens the sensitivity sums of rwnmr_cpmg_run_sens; with scratch the walk
+// carries its state in scratch buffers and leaves the context's walkers as they were
+rwnmr_status cpmg_impl(rwnmr_ctx *c, const rwnmr_cpmg_params *p, bool sens, bool scratch, double *echo_sum,
+                       uint64_t *echo_fx, uint64_t *echo_coll, double *echo_sens, uint64_t *echo_sens_fx)
 {
     RW_TRY(need_run_state(c));
     if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
@@ -582,7 +587,21 @@ rwnmr_status cpmg_impl(rwnmr_ctx *c, const rwnmr_cpmg_params *p, bool sens, doub
 
     int chunk = p->echoes_per_launch > 0 ? p->echoes_per_launch : std::max(32, (4096 / p->steps_per_echo) / 32 * 32);
     const DevImage im = c->image(p->bc, p->shift);
-    const WalkState st = c->state();
+    WalkState st = c->state();
+    if (scratch)
+    {
+        const size_t n1 = (size_t)std::max<int64_t>(c->n, 1);
+        RW_CUDA(c, c->rx.ensure(n1), "scratch state");
+        RW_CUDA(c, c->ry.ensure(n1), "scratch state");
+        RW_CUDA(c, c->rz.ensure(n1), "scratch state");
+        RW_CUDA(c, c->rseed.ensure(n1), "scratch state");
+        RW_CUDA(c, c->rcoll.ensure(n1 * slots), "scratch state");
+        st.x = c->rx.p;
+        st.y = c->ry.p;
+        st.z = c->rz.p;
+        st.seed = c->rseed.p;
+        st.coll = c->rcoll.p;
+    }
     CpmgLaunch L{};
     L.steps_per_echo = p->steps_per_echo;
     L.record = 1;
@@ -648,13 +667,13 @@ rwnmr_status cpmg_impl(rwnmr_ctx *c, const rwnmr_cpmg_params *p, bool sens, doub
 rwnmr_status rwnmr_cpmg_run(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *echo_sum, uint64_t *echo_fx,
                             uint64_t *echo_coll)
 {
-    return cpmg_impl(c, p, false, echo_sum, echo_fx, echo_coll, nullptr, nullptr);
+    return cpmg_impl(c, p, false, false, echo_sum, echo_fx, echo_coll, nullptr, nullptr);
 }
 
 rwnmr_status rwnmr_cpmg_run_sens(rwnmr_ctx *c, const rwnmr_cpmg_params *p, double *echo_sum, double *echo_sens,
                                  uint64_t *echo_sens_fx)
 {
-    return cpmg_impl(c, p, true, echo_sum, nullptr, nullptr, echo_sens, echo_sens_fx);
+    return cpmg_impl(c, p, true, false, echo_sum, nullptr, nullptr, echo_sens, echo_sens_fx);
 }
 
 // ---- internal field ---------------------------------------------------------------------------
@@ -810,6 +829,22 @@ rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const 
     if (p->n_echoes < 0 || p->steps_per_echo < 1) return c->fail(RWNMR_ERR_INVALID, "bad echo count / steps per echo");
     const int64_t nmax = (int64_t)p->n_echoes * p->steps_per_echo;
     if (nmax > (1ll << 28)) return c->fail(RWNMR_ERR_UNSUPPORTED, "walk too long");
+    bool positive = true;
+    for (int q = 0; q < c->n_phases; q++) positive = positive && p->dfactor[q] > 0.0;
+    if (positive)
+    {
+        // d echo_sum[e] / d f_q = (sum over walkers of E c_q) / f_q: one integer walk with the exact
+        // sensitivity sums, on scratch state; the FP64 replay below is for a zero factor
+        std::vector<double> sens((size_t)(p->n_echoes + 1) * c->n_phases);
+        RW_TRY(cpmg_impl(c, p, true, true, nullptr, nullptr, nullptr, sens.data(), nullptr));
+        for (int q = 0; q < c->n_phases; q++)
+        {
+            double s = 0.0;
+            for (int e = 1; e <= p->n_echoes; e++) s += grad_echo[e] * sens[(size_t)e * c->n_phases + q];
+            grad_dfactor[q] = s / p->dfactor[q];
+        }
+        return RWNMR_OK;
+    }
     cudaSetDevice(c->device);
     const int slots = phase_slots(c->n_phases);
     // derivative tables: dt[q][k] = k * f_q^(k-1) (so d/df_q of walker energy is dt[q][c_q] * prod_{r != q} t[r][c_r])
@@ -839,10 +874,6 @@ rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const 
     L.grad = c->grad.p;
     L.partial = c->partial.p;
     L.status = c->status.p;
-    // with every f_q > 0, dE/df_q = (c_q / f_q) E: the kernel sums g E c_q and the host divides
-    L.scaled = 1;
-    for (int q = 0; q < c->n_phases; q++)
-        if (!(p->dfactor[q] > 0.0)) L.scaled = 0;
     RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
     if (c->n > 0)
     {
@@ -863,7 +894,7 @@ rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const 
     {
         double s = 0.0;
         for (unsigned b = 0; b < grid.x; b++) s += part[(size_t)b * slots + q];
-        grad_dfactor[q] = L.scaled ? s / p->dfactor[q] : s;
+        grad_dfactor[q] = s;
     }
     // echo 0 does not depend on the decrease factors
     return RWNMR_OK;

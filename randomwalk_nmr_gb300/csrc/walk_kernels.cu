@@ -286,10 +286,9 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
 // (a few multiply-adds per walker-echo, no cross-lane FP64), then reduces once at the end.
 // partial: [gridDim.x][NP], summed on the host in block order (deterministic).
 // MORTON (noflux, no voxel division): the replay steps on the image's Morton copy.
-// SCALED (every f_q > 0): dE/df_q = (c_q / f_q) E, so the kernel accumulates sum_e g_e E(e) c_q(e) --
-// one energy product and one FMA per phase per walker-echo instead of a product per phase -- and
-// the host divides by f_q. The collision counts are kept as doubles as well, converted when they change.
-template <int BC, int NP, bool MORTON = false, bool SCALED = false>
+// This direct form serves decrease factors that include zero; with every f_q > 0 the host takes the
+// gradient from the forward walk's exact sensitivity sums instead (cpmg_walk_kernel, SENS).
+template <int BC, int NP, bool MORTON = false>
 __global__ void __launch_bounds__(kWalkThreads) cpmg_adjoint_kernel(DevImage im, WalkState st, AdjointLaunch L)
 {
     static_assert(!MORTON || BC == BC_NOFLUX, "the Morton walk is the noflux walk");
@@ -327,16 +326,12 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_adjoint_kernel(DevImage im,
     uint32_t P = 0; // MORTON: Morton index of the position
     if (MORTON && active)
         P = dilate_bits((uint32_t)p.x, im.mi.mx) | dilate_bits((uint32_t)p.y, im.mi.my) | dilate_bits((uint32_t)p.z, im.mi.mz);
-    double cd[NP]; // SCALED: collision counts as doubles
-#pragma unroll
-    for (int q = 0; q < NP; q++) cd[q] = 0.0;
     if (active)
     {
         const double *T = L.t;
         const double *dT = L.t + (size_t)NP * L.tstride;
         for (int e = 0; e < L.n_echoes; e++)
         {
-            uint32_t gained = 0; // SCALED: phases with collisions this echo
             for (int s = 0; s < L.steps_per_echo; s++)
             {
                 bool wall;
@@ -347,25 +342,9 @@ __global__ void __launch_bounds__(kWalkThreads) cpmg_adjoint_kernel(DevImage im,
                     walker_step<BC, W>(im, p, seed, wall, ph);
 #pragma unroll
                 for (int q = 0; q < NP; q++) c[q] += (wall && ph == q) ? 1u : 0u;
-                if (SCALED && wall) gained |= 1u << ph;
-            }
-            if (SCALED && gained)
-            {
-#pragma unroll
-                for (int q = 0; q < NP; q++)
-                    if (gained & (1u << q)) cd[q] = (double)c[q];
             }
             const double g = __ldg(L.grad + e + 1);
-            if (SCALED && g != 0.0)
-            {
-                double E = __ldg(T + c[0]);
-#pragma unroll
-                for (int q = 1; q < NP; q++) E *= __ldg(T + (size_t)q * L.tstride + c[q]);
-                const double G = g * E;
-#pragma unroll
-                for (int q = 0; q < NP; q++) acc[q] = fma(G, cd[q], acc[q]);
-            }
-            else if (!SCALED && g != 0.0)
+            if (g != 0.0)
             {
                 double tv[NP], dv[NP];
 #pragma unroll
@@ -777,10 +756,7 @@ cudaError_t launch_cpmg_adjoint(int bc_key, int np, const DevImage &im, const Wa
             constexpr int BC = decltype(bcc)::value;
             auto run = [&](auto mort) {
                 constexpr bool M = decltype(mort)::value;
-                if (L.scaled)
-                    cpmg_adjoint_kernel<BC, NP, M, true><<<grid, kWalkThreads, 0, s>>>(im, st, L);
-                else
-                    cpmg_adjoint_kernel<BC, NP, M, false><<<grid, kWalkThreads, 0, s>>>(im, st, L);
+                cpmg_adjoint_kernel<BC, NP, M><<<grid, kWalkThreads, 0, s>>>(im, st, L);
             };
             if constexpr (BC == BC_NOFLUX)
             {

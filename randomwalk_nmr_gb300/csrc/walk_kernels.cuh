@@ -72,7 +72,6 @@ struct AdjointLaunch
     const double *grad;  // [n_echoes + 1]
     double *partial;     // [gridDim.x][NP]
     unsigned *status;
-    int scaled;          // 1: partial holds sum g E c_q (every f_q > 0; the host divides by f_q)
 };
 
 struct PfgseLaunch

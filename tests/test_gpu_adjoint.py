@@ -146,3 +146,16 @@ def test_sensitivities_need_per_phase_factors(engine):
     engine.set_walker_dfactor(np.full(engine.n, 0.99))
     with pytest.raises(Exception, match="per-phase decrease factors"):
         engine.cpmg_sens(5, 2, None)
+
+
+@pytest.mark.parametrize("f", [[0.995, 0.98], [0.0, 0.98]])
+def test_adjoint_leaves_the_walkers(engine, f):
+    """Both adjoint paths (the integer sensitivity walk on scratch state, and the FP64 replay for a
+    zero factor) leave the context's walker state as the last walk left it."""
+    setup(engine, 2, n=500)
+    engine.cpmg(20, 2, [0.99, 0.97])
+    before = engine.download_walkers()
+    engine.cpmg_adjoint(35, 3, np.asarray(f), np.ones(36))
+    after = engine.download_walkers()
+    for key in before:
+        assert np.array_equal(before[key], after[key])
