@@ -364,10 +364,11 @@ def run_fit_batch(args):
     b.close()
 
 
-def pfgse_setup(small):
+def pfgse_setup(small, direction=(0.0, 0.0, 1.0)):
     """PFGSE diffusion workload: 256^3 sphere pack (radii 5-15, porosity 0.35, seed 3), 1M walkers
-    (SEED 7), rho 10 um/s, D0 2.5, 1 um voxels; 64 gradients linear 0-100 G/cm along z, delta 1 ms,
-    10 exposure times log-spaced 1-100 ms (15 ... 1500 steps, walked cumulatively)."""
+    (SEED 7), rho 10 um/s, D0 2.5, 1 um voxels; 64 gradients linear 0-100 G/cm along z (or along
+    `direction`), delta 1 ms, 10 exposure times log-spaced 1-100 ms (15 ... 1500 steps, walked
+    cumulatively)."""
     shape = (128, 128, 128) if small else (256, 256, 256)
     walkers = 100_000 if small else 1_000_000
     w = dict(name="pfgse-256" + ("-small" if small else ""), shape=shape, rmin=5.0, rmax=15.0, porosity=0.35,
@@ -378,8 +379,8 @@ def pfgse_setup(small):
     steps = np.array([max(1, int(round(d / dt))) for d in deltas], np.int32)
     n_g, gmax, pulse, gamma = 64, 100.0, 1.0, 42.576 * 2.0 * np.pi
     g = np.arange(n_g) * (gmax / (n_g - 1))
-    kvec = np.zeros((n_g, 3))
-    kvec[:, 2] = (pulse * 1e-3) * (gamma * 1e6) * (g * 1e-8)  # NMR_pfgse.cpp:483-486
+    d = np.asarray(direction, np.float64)
+    kvec = np.outer((pulse * 1e-3) * (gamma * 1e6) * (g * 1e-8), d / np.linalg.norm(d))  # NMR_pfgse.cpp:483-486
     f = 1.0 - (2.0 / 3.0) * (np.asarray(w["rho"]) * res) / (w["d0"] * 1e3)
     return w, res, steps, kvec, f, deltas
 
@@ -389,7 +390,8 @@ def run_pfgse(args):
 
     from randomwalk_nmr_gb300 import Engine
 
-    w, res, steps, kvec, f, deltas = pfgse_setup(args.workload.endswith("-small"))
+    direction = tuple(float(v) for v in args.gradient_direction.split(","))
+    w, res, steps, kvec, f, deltas = pfgse_setup(args.workload.endswith("-small"), direction)
     if args.impl == "reference":
         # reference arm: the reference's CPU PFGSE walk and phase sums (oracle port) on a bounded sample
         if int(os.environ.get("RANK", "0")) != 0:
@@ -495,7 +497,8 @@ def run_pfgse(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "int32/u64 walk, exact fixed-point energy histograms, f64 phase sums",
             "data": "synthetic sphere pack (no reference benchmark data)",
             "config": {"workload": w["name"], "image": "x".join(map(str, w["shape"])), "porosity": round(por, 4),
-                       "walkers": n, "gradients": int(len(kvec)), "exposure_times_ms": [round(float(d), 4) for d in deltas],
+                       "walkers": n, "gradients": int(len(kvec)), "gradient_direction": list(direction),
+                       "exposure_times_ms": [round(float(d), 4) for d in deltas],
                        "steps": [int(v) for v in steps], "walker_steps_per_step": steps_per_run,
                        "l2": "flushed (512 MB write) before every timed step", "parallelism": "1 GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -522,6 +525,8 @@ def main():
     ap.add_argument("--fit-evals", type=int, default=40)
     ap.add_argument("--fit-iters", type=int, default=6)
     ap.add_argument("--echoes", type=int, default=0, help="rho-fit-batch: echo count override (profiling)")
+    ap.add_argument("--gradient-direction", default="0,0,1",
+                    help="pfgse workloads: gradient direction x,y,z (an oblique one takes the general phase path)")
     ap.add_argument("--images", type=int, default=0, help="rho-fit-batch: use the first N images (profiling)")
     ap.add_argument("--batch-method", default="auto", choices=["auto", "histograms", "walk"],
                     help="rho-fit-batch: histogram evaluation (auto) or a candidate walk per fit iteration")

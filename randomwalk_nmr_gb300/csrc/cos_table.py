@@ -1,4 +1,4 @@
-"""Writes cos_table.inc: the constants of the field walk's fixed-point cosine (field_kernels.cu).
+"""Writes cos_table.inc: the constants of the fixed-point cosine (fixed_cos.cuh).
 
 Every value is computed in exact integer arithmetic: pi from Machin's formula
 pi = 16 atan(1/5) - 4 atan(1/239), sines and cosines from their Taylor series, all in fixed point

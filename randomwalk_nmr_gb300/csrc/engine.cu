@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/rwnmr_gb300.h"
+#include "fixed_cos.cuh"
 #include "walk_kernels.cuh"
 
 using namespace rwnmr;
@@ -111,6 +112,8 @@ struct rwnmr_ctx
     DevBuf<unsigned long long> acc, hist;
     DevBuf<unsigned> status;
     DevBuf<double> grad, partial, partial_g, kbuf, Mbuf, gbuf;
+    DevBuf<uint64_t> kappa;                  // general-direction PFGSE: k res / (2 pi) in turns
+    DevBuf<unsigned long long> dpart;        // general-direction PFGSE: exact block partials
     DevBuf<int32_t> ibuf, disp;
     DevBuf<double> energy;
 
@@ -283,6 +286,7 @@ void rwnmr_ctx_destroy(rwnmr_ctx *c)
     c->seed0.release(); c->seed.release(); c->coll.release();
     c->tfx.release(); c->tfp.release(); c->acc.release(); c->hist.release(); c->status.release();
     c->grad.release(); c->partial.release(); c->partial_g.release(); c->kbuf.release(); c->Mbuf.release();
+    c->kappa.release(); c->dpart.release();
     c->gbuf.release(); c->ibuf.release(); c->disp.release(); c->energy.release();
     c->wf.release(); c->wenergy.release(); c->field.release(); c->phase.release(); c->btab.release();
     c->rx.release(); c->ry.release(); c->rz.release(); c->rseed.release(); c->rcoll.release();
@@ -1063,8 +1067,8 @@ static rwnmr_status pfgse_impl(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double
                                      walk_grid(c->n), c->stream), "pfgse kernel");
         c->launches++;
     }
-    RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
-    // phase sums
+    // phase sums (the timed region ends after them)
+    bool timed = false;
     std::vector<double> Mh((size_t)nd * ng, 0.0), Gh((size_t)nd * ng, 0.0);
     if (nd > 0 && ng > 0)
     {
@@ -1086,6 +1090,8 @@ static rwnmr_status pfgse_impl(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double
             PL.dMdg = want_grad ? c->gbuf.p : nullptr;
             RW_CUDA(c, launch_pfgse_phase(PL, nd, ng, c->stream), "phase kernel");
             c->launches++;
+            RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
+            timed = true;
             RW_CUDA(c, cudaMemcpyAsync(Mh.data(), c->Mbuf.p, Mh.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
             if (want_grad)
                 RW_CUDA(c, cudaMemcpyAsync(Gh.data(), c->gbuf.p, Gh.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
@@ -1093,45 +1099,61 @@ static rwnmr_status pfgse_impl(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double
         else if (c->n > 0)
         {
             const int blocks = (int)std::min<int64_t>(1184, (c->n + 255) / 256);
-            RW_CUDA(c, c->kbuf.ensure((size_t)ng * 3), "k buffer");
-            RW_CUDA(c, cudaMemcpyAsync(c->kbuf.p, p->kvec, (size_t)ng * 24, cudaMemcpyHostToDevice, c->stream), "k upload");
-            RW_CUDA(c, c->partial.ensure((size_t)nd * ng * blocks), "partials");
+            // k_ja res / (2 pi) mod 1 in 2^-64 turns, from the exact product k res (two FP64 terms)
+            std::vector<uint64_t> kappa((size_t)ng * 3);
+            for (size_t k = 0; k < kappa.size(); k++)
+            {
+                const double hi = p->kvec[k] * p->res, lo = std::fma(p->kvec[k], p->res, -hi);
+                kappa[k] = fxcos::turns_q64_host(hi) + fxcos::turns_q64_host(lo);
+            }
+            RW_CUDA(c, c->kappa.ensure(kappa.size()), "k buffer");
+            RW_CUDA(c, cudaMemcpyAsync(c->kappa.p, kappa.data(), kappa.size() * 8, cudaMemcpyHostToDevice, c->stream),
+                    "k upload");
+            RW_CUDA(c, c->dpart.ensure((size_t)nd * ng * blocks * 3), "partials");
             RW_CUDA(c, c->partial_g.ensure((size_t)nd * ng * blocks), "partials");
             DirectLaunch DL{};
             DL.n = c->n;
             DL.n_g = ng;
             DL.disp = c->disp.p;
             DL.energy = c->energy.p;
-            DL.kvec = c->kbuf.p;
+            DL.kappa = c->kappa.p;
             DL.res = p->res;
             DL.grad_on = want_grad ? 1 : 0;
             DL.kscale = kscale;
             for (int a = 0; a < 3; a++) DL.dir[a] = dir ? dir[a] : 0.0;
-            DL.partial = c->partial.p;
+            DL.partial = c->dpart.p;
             DL.partial_g = c->partial_g.p;
             RW_CUDA(c, launch_pfgse_direct(DL, nd, blocks, c->stream), "direct phase kernel");
             c->launches++;
-            std::vector<double> part((size_t)nd * ng * blocks), partg;
-            RW_CUDA(c, cudaMemcpyAsync(part.data(), c->partial.p, part.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
+            RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
+            timed = true;
+            std::vector<unsigned long long> part((size_t)nd * ng * blocks * 3);
+            std::vector<double> partg;
+            RW_CUDA(c, cudaMemcpyAsync(part.data(), c->dpart.p, part.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
             if (want_grad)
             {
-                partg.resize(part.size());
+                partg.resize((size_t)nd * ng * blocks);
                 RW_CUDA(c, cudaMemcpyAsync(partg.data(), c->partial_g.p, partg.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
             }
             RW_CUDA(c, cudaStreamSynchronize(c->stream), "readback");
+            // every walker added E cos 2^61 + 2^61 for every (i, j): exact sums, offset removed
+            const __int128 offset = (__int128)c->n << 61;
             for (size_t k = 0; k < (size_t)nd * ng; k++)
             {
-                double s = 0.0, g = 0.0;
+                __int128 v = -offset;
+                double g = 0.0;
                 for (int b = 0; b < blocks; b++)
                 {
-                    s += part[k * blocks + b];
+                    const unsigned long long *l = &part[(k * blocks + b) * 3];
+                    v += (__int128)l[0] + ((__int128)l[1] << 21) + ((__int128)l[2] << 42);
                     if (want_grad) g += partg[k * blocks + b];
                 }
-                Mh[k] = s;
+                Mh[k] = std::ldexp((double)v, -61);
                 Gh[k] = g;
             }
         }
     }
+    if (!timed) RW_CUDA(c, cudaEventRecord(c->ev1, c->stream), "event");
     std::vector<unsigned long long> acc((size_t)nd * 6);
     if (nd) RW_CUDA(c, cudaMemcpyAsync(acc.data(), c->acc.p, acc.size() * 8, cudaMemcpyDeviceToHost, c->stream), "readback");
     RW_TRY(c->check_status("pfgse walk"));

@@ -20,14 +20,16 @@
 //   * the only FP64 arithmetic per echo is the reference's phase updates (two FMAs per step, kept bit
 //     for bit). E = pAlive * cos(phase) is evaluated in 64-bit integer arithmetic, since FP64 is the
 //     slow pipe of this GPU and its integer pipes are nearly idle here: pAlive from the fixed-point
-//     survival tables (or the per-walker FP64 product converted exactly), cos(phase) by a fixed-point
-//     Payne-Hanek-style reduction to turns, a 1024-entry quadrant table and Taylor terms. The absolute
-//     error of E is below 2^-59.5 for |phase| < 2^40 (the reference's FP64 cos itself rounds at up
-//     to 2^-53); larger or non-finite phases take CUDA's cos.
+//     survival tables (or the per-walker FP64 product converted exactly), cos(phase) by the
+//     fixed-point cosine of fixed_cos.cuh (a Payne-Hanek-style reduction to turns, a 1024-entry
+//     quadrant table and Taylor terms). The absolute error of E is below 2^-59.5 for |phase| < 2^40
+//     (the reference's FP64 cos itself rounds at up to 2^-53); larger or non-finite phases take
+//     CUDA's cos.
 #include <cstdint>
 #include <type_traits>
 #include <cuda_runtime.h>
 
+#include "fixed_cos.cuh"
 #include "walk_device.cuh"
 #include "walk_kernels.cuh"
 
@@ -79,74 +81,6 @@ __device__ __forceinline__ uint64_t energy_offset_fx(double e)
     return (uint64_t)(v + (1ll << 61));
 }
 
-#include "cos_table.inc"
-
-// cos(phase) * 2^62 as a signed integer, for |phase| < 2^40 (false otherwise: larger, inf, nan).
-//   1. theta = |phase| / (2 pi) mod 1 in units of 2^-66 turns: the 53-bit mantissa times 2^128 / (2 pi)
-//      (two words) and the exponent's window of the product (the idea of Payne and Hanek's reduction,
-//      a fixed window of the constant being enough below 2^40); error below 2^-66 turns.
-//   2. k = theta rounded to 1/4096 turn, r = 2 pi (theta - k / 4096) with |r| <= pi / 4096.
-//   3. cos(k pi / 2048 + r) from the quadrant k / 1024, the table cos / sin (j pi / 2048), j = k mod 1024,
-//      and cos r = 1 - r^2/2 + r^4/24, sin r = r - r^3/6 + r^5/120 (the next terms are below 2^-71):
-//      r and r^2 in 64-bit fixed point, the higher terms in 32-bit multiplies.
-// Measured against exact values (cos_table.py's 256-bit arithmetic): error below 2.1 units of 2^-62.
-__device__ __forceinline__ bool cos_q62(double phase, const ulonglong2 *__restrict__ quad, long long &out)
-{
-    const uint64_t bits = (uint64_t)__double_as_longlong(phase);
-    const int ex = (int)((bits >> 52) & 0x7ff);
-    if (ex >= 1063) return false;
-    const int sh = 1139 - ex; // theta = (mantissa * 2^128 / (2 pi)) >> sh, modulo 2^64
-    uint64_t theta = 0;
-    uint32_t g = 0; // the next two bits of the product (2^-65, 2^-66 turns)
-    if (ex != 0 && sh < 178)
-    {
-        const uint64_t m = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-        const uint64_t lo2 = m * INV_2PI_HI;
-        const uint64_t q1 = __umul64hi(m, INV_2PI_LO) + lo2;
-        const uint64_t q2 = __umul64hi(m, INV_2PI_HI) + (q1 < lo2 ? 1 : 0);
-        theta = sh < 128 ? (q1 >> (sh - 64)) | (q2 << (128 - sh)) : q2 >> (sh - 128);
-        g = (uint32_t)(sh < 130 ? q1 >> (sh - 66) : q2 >> (sh - 130)) & 3u;
-    }
-    const uint64_t tr = theta + (1ull << 51);
-    const int k = (int)(tr >> 52);
-    const long long d = (long long)(theta - (tr & ~((1ull << 52) - 1))) * 4 + g; // [-2^53, 2^53)
-    const bool neg_r = d < 0;
-    const uint64_t a = (uint64_t)(neg_r ? -d : d);
-    const uint64_t R = __umul64hi(a << 10, TWO_PI_Q61); // |r| 2^73
-    const uint64_t u = __umul64hi(R, R);                // r^2 2^82
-    const uint32_t u32 = (uint32_t)(u >> 31);           // r^2 2^51
-    const uint32_t r32 = (uint32_t)(R >> 31);           // |r| 2^42
-    const uint32_t hi3 = __umulhi(r32, u32);            // |r|^3 2^61
-    // 1 - cos r = r^2/2 - r^4/24 (times 2^63); p1 = A cos r = A/2 - A (1 - cos r), each a two-term
-    // difference (the fused form 2^63 - x + t came out wrong on sm_103a when x = t = 0)
-    const uint64_t dev = (u >> 20) - __umulhi(__umulhi(u32, u32), C_INV3072);
-    const uint64_t sr = R - (((uint64_t)hi3 * C_INV6) >> 20) + __umulhi(__umulhi(hi3, u32), C_INV15360); // |sin r| 2^73
-    const ulonglong2 cs = quad[k & (kQuadrant - 1)];
-    const bool odd = (k >> 10) & 1;
-    // quadrants 0..3: cos(phi), -sin(phi), -cos(phi), sin(phi) with phi = j pi / 2048 + r
-    const uint64_t A = odd ? cs.y : cs.x;
-    const long long p1 = (long long)((A >> 1) - __umul64hi(A, dev));
-    const long long p2 = (long long)((__umul64hi(odd ? cs.x : cs.y, sr) + 512) >> 10);
-    const long long v = odd == neg_r ? p1 - p2 : p1 + p2;
-    out = (((k >> 10) + 1) & 2) ? -v : v;
-    return true;
-}
-
-// round(p * 2^63), half to even (the survival tables' rounding), for an FP64 probability p in
-// [0, 1], from its bits.
-__device__ __forceinline__ uint64_t prob_q63(double p)
-{
-    const uint64_t bits = (uint64_t)__double_as_longlong(p);
-    const int ex = (int)((bits >> 52) & 0x7ff);
-    if (ex < 959) return 0; // below 2^-64
-    const uint64_t m = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-    const int sh = ex - 1012; // p 2^63 = m 2^(ex - 1075 + 63), sh <= 11
-    if (sh >= 0) return m << sh;
-    const int r = -sh; // 1 .. 53
-    const uint64_t q = m >> r, rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
-    return q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
-}
-
 // The echo term E * 2^61 + 2^61 of a walker with survival probability pal63 / 2^63 and phase `phase`.
 // pal_fp64() is the same probability as an FP64 number, used only when cos_q62 declines the phase.
 template <typename PalFp64>
@@ -154,7 +88,7 @@ __device__ __forceinline__ uint64_t echo_term(double phase, uint64_t pal63, PalF
                                               const ulonglong2 *__restrict__ quad)
 {
     long long c62;
-    if (!cos_q62(phase, quad, c62)) return energy_offset_fx(pal_fp64() * cos(phase));
+    if (!fxcos::cos_q62(phase, quad, c62)) return energy_offset_fx(pal_fp64() * cos(phase));
     const uint64_t m = __umul64hi(pal63, (uint64_t)(c62 < 0 ? -c62 : c62)); // pal |cos| 2^61
     return (uint64_t)((c62 < 0 ? -(long long)m : (long long)m) + (1ll << 61));
 }
@@ -180,7 +114,7 @@ __global__ void __launch_bounds__(kWalkThreads, MORTON ? 6 : 4) cpmg_field_kerne
     constexpr int W = WordsPerBlock<NP>::value;
     constexpr int K = 3;
     __shared__ unsigned long long sacc[32 * K];
-    __shared__ ulonglong2 quad[kQuadrant]; // 16 KB: cos / sin of the first quadrant
+    __shared__ ulonglong2 quad[fxcos::kQuadrant]; // 16 KB: cos / sin of the first quadrant
     __shared__ uint4 sdir[6];              // MORTON: direction table
     if (MORTON && threadIdx.x < 6) sdir[threadIdx.x] = morton_direction(im.mi, threadIdx.x);
 
@@ -240,11 +174,10 @@ __global__ void __launch_bounds__(kWalkThreads, MORTON ? 6 : 4) cpmg_field_kerne
     }
 
     for (int k = threadIdx.x; k < 32 * K; k += blockDim.x) sacc[k] = 0;
-    for (int k = threadIdx.x; k < kQuadrant; k += blockDim.x)
-        quad[k] = make_ulonglong2(kQuadrantCosSin[k][0], kQuadrantCosSin[k][1]);
+    fxcos::load_quadrant_table(quad);
     __syncthreads();
     // pAlive as 2^63 fixed point: the survival tables, or the walker's own FP64 product converted
-    auto pal_q63 = [&]() { return WF ? prob_q63(pa) : energy_fx<NP>(L.tfx, L.tstride, c); };
+    auto pal_q63 = [&]() { return WF ? fxcos::prob_q63(pa) : energy_fx<NP>(L.tfx, L.tstride, c); };
     auto pal_fp64 = [&]() { return WF ? pa : ldexp((double)energy_fx<NP>(L.tfx, L.tstride, c), -63); };
     if (L.e_begin == 0)
     {

@@ -19,6 +19,7 @@
 #include <type_traits>
 #include <cuda_runtime.h>
 
+#include "fixed_cos.cuh"
 #include "walk_device.cuh"
 #include "walk_kernels.cuh"
 
@@ -563,54 +564,117 @@ __global__ void pfgse_phase_kernel(PhaseLaunch L)
     }
 }
 
-// General gradient direction: per-walker cos((k_j . dR) res) E. Block partials, fixed-order
-// host-side finish: partial[(i * n_g + j) * gridDim.x + block].
-__global__ void pfgse_direct_kernel(DirectLaunch L)
+// PFGSE phase sums for a general gradient direction: M_ij = sum_w E_w cos(k_j . dR_w res) for every
+// walker w (its displacement dR and energy at exposure time i, stored by the walk), and with grad_on
+// dM_ij/dg = -sum_w E_w sin(k_j . dR_w res) kscale (dir . dR_w) res. The angle is formed in turns from
+// the host's kappa_ja = k_ja res / (2 pi) mod 1 (2^-64 turns): theta = sum_a dR_a kappa_ja modulo one
+// turn, exact integer arithmetic with no reduction step; cos and sin come from the fixed-point
+// cosine (fixed_cos.cuh). Each walker adds E cos * 2^61 + 2^61 (E as round(E 2^63)), summed exactly as
+// three 21-bit limbs through redux.sync; lane l keeps the sums of gradient points j = 32 s + l. The
+// gradient sums stay FP64 (E sin times the walker's projection), reduced in a fixed order.
+// grid (blocks, n_delta) x 256 threads; each warp takes 32 walkers at a time.
+__global__ void __launch_bounds__(256) pfgse_direct_kernel(DirectLaunch L)
 {
-    const int i = blockIdx.y;
-    double accs[kDirectMaxG];
-    double accg[kDirectMaxG];
+    __shared__ ulonglong2 quad[fxcos::kQuadrant];
+    __shared__ uint64_t skap[kDirectMaxG][3];
+    __shared__ unsigned long long sacc[kDirectMaxG][3];
+    __shared__ double sgw[8][kDirectMaxG];
+    fxcos::load_quadrant_table(quad);
     const int ng = L.n_g;
-    for (int j = 0; j < ng; j++)
+    for (int k = threadIdx.x; k < ng * 3; k += blockDim.x)
     {
-        accs[j] = 0.0;
-        accg[j] = 0.0;
+        skap[k / 3][k % 3] = L.kappa[k];
+        sacc[k / 3][k % 3] = 0;
     }
-    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < L.n; w += (int64_t)gridDim.x * blockDim.x)
+    __syncthreads();
+    const int i = blockIdx.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NS = kDirectMaxG / 32;
+    unsigned long long acc[NS][3];
+    double gacc[NS];
+#pragma unroll
+    for (int s = 0; s < NS; s++)
     {
-        const size_t o = (size_t)i * L.n + w;
-        const double dX = (double)L.disp[o * 3 + 0], dY = (double)L.disp[o * 3 + 1], dZ = (double)L.disp[o * 3 + 2];
-        const double e = L.energy[o];
-        for (int j = 0; j < ng; j++)
+        acc[s][0] = acc[s][1] = acc[s][2] = 0;
+        gacc[s] = 0.0;
+    }
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + warp * 32; base < L.n; base += stride)
+    {
+        const int64_t w = base + lane;
+        const bool active = w < L.n;
+        int32_t d0 = 0, d1 = 0, d2 = 0;
+        uint64_t e63 = 0;
+        double pr = 0.0; // grad_on: kscale (dir . dR) res 2^-61
+        if (active)
         {
-            const double kd = L.kvec[3 * j] * dX + L.kvec[3 * j + 1] * dY + L.kvec[3 * j + 2] * dZ;
-            double sn, cs;
-            sincos(kd * L.res, &sn, &cs);
-            accs[j] += e * cs;
+            const size_t o = (size_t)i * L.n + w;
+            d0 = L.disp[o * 3 + 0];
+            d1 = L.disp[o * 3 + 1];
+            d2 = L.disp[o * 3 + 2];
+            e63 = fxcos::prob_q63(L.energy[o]);
             if (L.grad_on)
-            {
-                const double proj = L.kscale * (L.dir[0] * dX + L.dir[1] * dY + L.dir[2] * dZ);
-                accg[j] -= e * sn * proj * L.res;
-            }
+                pr = L.kscale * (L.dir[0] * (double)d0 + L.dir[1] * (double)d1 + L.dir[2] * (double)d2) * L.res *
+                     0x1p-61;
         }
-    }
-    __shared__ double red[256];
-    for (int j = 0; j < ng; j++)
-    {
-        for (int which = 0; which < (L.grad_on ? 2 : 1); which++)
+#pragma unroll
+        for (int s = 0; s < NS; s++)
         {
-            red[threadIdx.x] = which ? accg[j] : accs[j];
-            __syncthreads();
-            for (int o = blockDim.x / 2; o > 0; o >>= 1)
+            for (int jj = 0; jj < 32; jj++)
             {
-                if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-                __syncthreads();
+                const int j = 32 * s + jj;
+                if (j >= ng) break;
+                const uint64_t theta = (uint64_t)(int64_t)d0 * skap[j][0] + (uint64_t)(int64_t)d1 * skap[j][1] +
+                                       (uint64_t)(int64_t)d2 * skap[j][2];
+                long long c62, s62 = 0;
+                if (L.grad_on)
+                    fxcos::sincos_turns_q62(theta, 0, quad, c62, s62);
+                else
+                    c62 = fxcos::cos_turns_q62(theta, 0, quad);
+                const uint64_t m = __umul64hi(e63, (uint64_t)(c62 < 0 ? -c62 : c62)); // E |cos| 2^61
+                const uint64_t u = active ? (uint64_t)((c62 < 0 ? -(long long)m : (long long)m) + (1ll << 61)) : 0;
+                const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(u & M21));
+                const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((u >> 21) & M21));
+                const uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(u >> 42));
+                if (lane == jj)
+                {
+                    acc[s][0] += r0;
+                    acc[s][1] += r1;
+                    acc[s][2] += r2;
+                }
+                if (L.grad_on)
+                {
+                    const uint64_t ms = __umul64hi(e63, (uint64_t)(s62 < 0 ? -s62 : s62)); // E |sin| 2^61
+                    double v = -(double)(s62 < 0 ? -(long long)ms : (long long)ms) * pr;
+                    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+                    v = __shfl_sync(FULL, v, 0);
+                    if (lane == jj) gacc[s] += v;
+                }
             }
-            if (threadIdx.x == 0)
-                (which ? L.partial_g : L.partial)[((size_t)i * ng + j) * gridDim.x + blockIdx.x] = red[0];
-            __syncthreads();
         }
     }
+#pragma unroll
+    for (int s = 0; s < NS; s++)
+    {
+        const int j = 32 * s + lane;
+        if (j < ng)
+        {
+            atomicAdd(&sacc[j][0], acc[s][0]);
+            atomicAdd(&sacc[j][1], acc[s][1]);
+            atomicAdd(&sacc[j][2], acc[s][2]);
+            sgw[warp][j] = gacc[s];
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < ng * 3; k += blockDim.x)
+        L.partial[(((size_t)i * ng + k / 3) * gridDim.x + blockIdx.x) * 3 + k % 3] = sacc[k / 3][k % 3];
+    if (L.grad_on)
+        for (int j = threadIdx.x; j < ng; j += blockDim.x)
+        {
+            double v = 0.0;
+            for (int wv = 0; wv < 8; wv++) v += sgw[wv][j];
+            L.partial_g[((size_t)i * ng + j) * gridDim.x + blockIdx.x] = v;
+        }
 }
 
 // Packs a label volume into bit-blocks with phase planes (BitBlock/bitBlock.cpp:138-221 plus the

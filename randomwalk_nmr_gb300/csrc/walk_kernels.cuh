@@ -108,13 +108,13 @@ struct DirectLaunch
     int n_g;
     const int32_t *disp;
     const double *energy;
-    const double *kvec; // device [n_g][3]
+    const uint64_t *kappa; // device [n_g][3]: k_ja res / (2 pi) mod 1, in 2^-64 turns
     double res;
     int grad_on;
     double kscale;
     double dir[3];
-    double *partial;   // [n_delta][n_g][blocks]
-    double *partial_g; // [n_delta][n_g][blocks]
+    unsigned long long *partial; // [n_delta][n_g][blocks][3]: limbs of sum (E cos 2^61 + 2^61)
+    double *partial_g;           // [n_delta][n_g][blocks]
 };
 
 cudaError_t launch_cpmg_walk(int bc_key, int np, const DevImage &im, const WalkState &st, const CpmgLaunch &L,

@@ -1,7 +1,8 @@
-"""The field walk's fixed-point cosine (field_kernels.cu: cos_q62, prob_q63) restated step for step in
-Python integers, against exact values from cos_table.py's 256-bit arithmetic, and the committed
-constant file against its generator. The GPU's own results are checked against the same exact values
-in test_gpu_field.py."""
+"""The fixed-point cosine and sine (fixed_cos.cuh: turns_of, cos_turns_q62, sincos_turns_q62,
+prob_q63, turns_q64_host) restated step for step in Python integers, against exact values from
+cos_table.py's 256-bit arithmetic, and the committed constant file against its generator. The GPU's
+own results are checked against the same exact values in test_gpu_field.py (internal-field walk) and
+through the general-direction PFGSE parity tests."""
 import math
 import os
 import random
@@ -30,8 +31,8 @@ def umulhi32(a, b):
     return (a * b) >> 32
 
 
-def cos_q62(phase):
-    """field_kernels.cu cos_q62, line by line; None where the kernel falls back to CUDA's cos."""
+def turns_of(phase):
+    """fixed_cos.cuh turns_of: (theta, g) or None where the kernels fall back to CUDA's cos."""
     bits = struct.unpack("<Q", struct.pack("<d", phase))[0]
     ex = (bits >> 52) & 0x7FF
     if ex >= 1063:
@@ -45,6 +46,11 @@ def cos_q62(phase):
         q2 = (umulhi(m, C["INV_2PI_HI"]) + (1 if q1 < lo2 else 0)) & M64
         theta = ((q1 >> (sh - 64)) | (q2 << (128 - sh))) & M64 if sh < 128 else q2 >> (sh - 128)
         g = ((q1 >> (sh - 66)) if sh < 130 else (q2 >> (sh - 130))) & 3
+    return theta, g
+
+
+def turn_parts(theta, g):
+    """fixed_cos.cuh turn_parts: (C, S, dev, sr, quadrant, neg_r)."""
     tr = (theta + (1 << 51)) & M64
     k = tr >> 52
     d = (theta - (tr & ~((1 << 52) - 1))) & M64
@@ -58,12 +64,58 @@ def cos_q62(phase):
     dev = (u >> 20) - umulhi32(umulhi32(u32, u32), C["C_INV3072"])
     sr = R - ((hi3 * C["C_INV6"]) >> 20) + umulhi32(umulhi32(hi3, u32), C["C_INV15360"])
     cj, sj = C["table"][k & (cos_table.QUADRANT - 1)]
-    odd = (k >> 10) & 1
-    A = sj if odd else cj
-    p1 = (A >> 1) - umulhi(A, dev)
-    p2 = (umulhi(cj if odd else sj, sr) + 512) >> 10
+    return cj, sj, dev, sr, (k >> 10) & 3, neg_r
+
+
+def mul_cos_r(A, dev):
+    return (A >> 1) - umulhi(A, dev)
+
+
+def mul_sin_r(A, sr):
+    return (umulhi(A, sr) + 512) >> 10
+
+
+def cos_turns_q62(theta, g=0):
+    cj, sj, dev, sr, q, neg_r = turn_parts(theta, g)
+    odd = q & 1
+    p1 = mul_cos_r(sj if odd else cj, dev)
+    p2 = mul_sin_r(cj if odd else sj, sr)
     v = p1 - p2 if bool(odd) == neg_r else p1 + p2
-    return -v if ((k >> 10) + 1) & 2 else v
+    return -v if (q + 1) & 2 else v
+
+
+def sincos_turns_q62(theta, g=0):
+    cj, sj, dev, sr, q, neg_r = turn_parts(theta, g)
+    cc, sc = mul_cos_r(cj, dev), mul_cos_r(sj, dev)
+    cs, ss = mul_sin_r(cj, sr), mul_sin_r(sj, sr)
+    cphi = cc + ss if neg_r else cc - ss
+    sphi = sc - cs if neg_r else sc + cs
+    odd, high = bool(q & 1), bool(q & 2)
+    c0, s0 = (sphi, cphi) if odd else (cphi, sphi)
+    return (-c0 if odd != high else c0), (-s0 if high else s0)
+
+
+def cos_q62(phase):
+    """fixed_cos.cuh cos_q62; None where the kernels fall back to CUDA's cos."""
+    t = turns_of(phase)
+    return None if t is None else cos_turns_q62(*t)
+
+
+def turns_q64_host(x):
+    """fixed_cos.cuh turns_q64_host."""
+    ax = abs(x)
+    bits = struct.unpack("<Q", struct.pack("<d", ax))[0]
+    ex = bits >> 52
+    if ex == 0 or ex >= 1063:
+        return 0
+    s = 1139 - ex - 66
+    if s >= 128:
+        return 0
+    m = (bits & ((1 << 52) - 1)) | (1 << 52)
+    W = ((m * C["INV_2PI_LO"]) >> 64) + m * C["INV_2PI_HI"]
+    t66 = (W >> s) & ((1 << 66) - 1)
+    theta = ((t66 + 2) >> 2) & M64
+    return (-theta) & M64 if x < 0 else theta
 
 
 def prob_q63(p):
@@ -90,6 +142,16 @@ def exact_cos_q62(phase):
     q = x // half_pi
     c, s = cos_table.cos_sin(x - q * half_pi)
     return Fraction([c, -s, -c, s][q % 4] << 62, 1 << cos_table.BITS)
+
+
+def exact_sincos_turns_q62(t):
+    """(cos, sin)(2 pi t) * 2^62 as exact fractions, t a Fraction of a turn."""
+    t = t - (t.numerator // t.denominator)
+    q4 = t * 4
+    q = q4.numerator // q4.denominator
+    c, s = cos_table.cos_sin(int((q4 - q) * (cos_table.PI // 2)))  # the angle within its quadrant
+    cv, sv = [(c, s), (-s, c), (-c, -s), (s, -c)][q % 4]
+    return Fraction(cv << 62, 1 << cos_table.BITS), Fraction(sv << 62, 1 << cos_table.BITS)
 
 
 def test_constant_file_matches_generator():
@@ -163,3 +225,36 @@ def test_echo_term_error_bound(seed):
         m = umulhi(pal, abs(c62))
         e = -m if c62 < 0 else m
         assert abs(e - Fraction(pal, 1 << 63) * exact_cos_q62(x) / 2) < 3
+
+
+def test_sincos_in_turns_error_bound():
+    rng = random.Random(21)
+    thetas = [0, 1, (1 << 64) - 1, 1 << 62, 1 << 63, 3 << 62, 1 << 52, (1 << 52) - 1, 1 << 51, (1 << 51) + 1]
+    thetas += [k << 52 for k in range(0, 4096, 97)] + [(k << 52) + rng.randint(-3, 3) for k in range(0, 4096, 131)]
+    thetas += [rng.getrandbits(64) for _ in range(4000)]
+    worst = Fraction(0)
+    for th in thetas:
+        th &= M64
+        for g in (0, 3):
+            c, s_ = sincos_turns_q62(th, g)
+            assert c == cos_turns_q62(th, g)
+            ec, es = exact_sincos_turns_q62(Fraction(th * 4 + g, 1 << 66))
+            worst = max(worst, abs(c - ec), abs(s_ - es))
+    assert worst < BOUND_Q62, float(worst)
+
+
+def test_host_turns_exact_to_a_unit():
+    """turns_q64_host(x) within one unit of 2^64 frac(x / (2 pi)), for both signs."""
+    rng = random.Random(8)
+    xs = [1.0, -1.0, math.pi, 2 * math.pi, 1e-3, -1e-3, 0.1234, 5e-20, 1e6 + 0.5, -(2.0 ** 39)]
+    xs += [rng.uniform(-1e4, 1e4) for _ in range(500)] + [rng.uniform(-1e-6, 1e-6) for _ in range(100)]
+    two_pi = Fraction(2 * cos_table.PI, 1 << cos_table.BITS)
+    for x in xs:
+        t = Fraction(x) / two_pi
+        t -= t.numerator // t.denominator
+        exact = t * (1 << 64)
+        got = turns_q64_host(x)
+        diff = abs(got - exact)
+        diff = min(diff, abs(diff - (1 << 64)))  # the turn wraps
+        assert diff <= 1, (x, float(diff))
+    assert turns_q64_host(0.0) == 0 and turns_q64_host(2.0 ** 41) == 0

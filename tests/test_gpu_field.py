@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from conftest import dfactor
-from test_field_cos import exact_cos_q62
+from test_fixed_cos import exact_cos_q62
 from randomwalk_nmr_gb300 import RwnmrError, host
 
 pytestmark = pytest.mark.gpu
