@@ -1012,6 +1012,11 @@ static rwnmr_status pfgse_impl(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double
         }
         if (p->n_g > kDirectMaxG && axis < 0)
             return c->fail(RWNMR_ERR_UNSUPPORTED, "general-direction PFGSE handles at most %d gradient points", kDirectMaxG);
+        if (axis < 0)
+            for (int k = 0; k < 3 * p->n_g; k++)
+                if (!(std::fabs(p->kvec[k] * p->res) < 0x1p40))
+                    return c->fail(RWNMR_ERR_UNSUPPORTED, "general-direction PFGSE needs |k res| < 2^40 (got %g)",
+                                   p->kvec[k] * p->res);
     }
     const int slots = phase_slots(c->n_phases);
     std::vector<uint64_t> fx;

@@ -249,3 +249,22 @@ def test_field_walk_layouts_identical(engine, n_phases):
         for key in ("x", "y", "z", "seed", "collisions"):
             assert np.array_equal(sa[key], sb[key])
     engine.allow_morton(True)
+
+
+def test_field_huge_phases_take_the_fp64_cosine(engine, oracle):
+    """Phases of 2^40 rad and more (a field far beyond any physical one) leave the fixed-point
+    cosine's range; those walkers' energies take CUDA's FP64 cos, and the sums still match the
+    oracle's."""
+    lab = image(seed=17)
+    w = walkers(lab, 1200, 3)
+    n = len(w[0])
+    engine.upload_labels(lab)
+    engine.upload_walkers(*w)
+    gradient = 1.0e15  # T/m: a move along x changes gammatau * B by ~2^43 rad
+    engine.set_field_uniform(gradient, 0, RES)
+    g = engine.cpmg_field(6, 2, dfactor(10.0), GAMMA, TIME_INTERVAL)
+    assert np.mean(np.abs(g["phase"]) >= 2.0 ** 40) > 0.2
+    st = engine.download_walkers()
+    o = oracle.cpmg_field(lab, w, 6, 2, dfactor(10.0), 0.5 * GAMMA * TIME_INTERVAL, dg=gradient * 1.0e-6 * RES,
+                          axis=0, threads=4)
+    assert_parity(g, st, o, n)

@@ -127,3 +127,11 @@ def test_pfgse_per_walker_dfactor(engine, golden):
         a = engine.pfgse(steps, kv, 1.0, f)
         b = engine.pfgse(steps, kv, 1.0, None)
         assert np.array_equal(a["esum"], b["esum"]) and np.array_equal(a["M"], b["M"])
+
+
+def test_pfgse_general_direction_rejects_huge_wavevectors(engine):
+    setup(engine)
+    kv = kvecs(4, (30.0, 40.0, 20.0))
+    kv[-1] *= 1e16
+    with pytest.raises(Exception, match="k res"):
+        engine.pfgse(np.array([10, 20], np.int32), kv, 1.0, dfactor(10.0))
