@@ -24,6 +24,7 @@
 #ifndef RWNMR_GB300_H
 #define RWNMR_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -38,7 +39,9 @@ typedef enum rwnmr_status
     RWNMR_ERR_NOMEM = 3,       /* device allocation failed */
     RWNMR_ERR_STATE = 4,       /* call out of order (e.g. no image uploaded) */
     RWNMR_ERR_UNSUPPORTED = 5, /* valid request this build does not handle */
-    RWNMR_ERR_DEVICE = 6       /* the kernel reported a fault through its status word */
+    RWNMR_ERR_DEVICE = 6,      /* the kernel reported a fault through its status word */
+    RWNMR_ERR_CANCELLED = 7,   /* a batch walk stopped on rwnmr_batch_cancel (no results) */
+    RWNMR_ERR_TIMEOUT = 8      /* a batch walk stopped at its time budget (no results) */
 } rwnmr_status;
 
 /* Boundary conditions (rwnmr.config BC; ConfigFiles/rwnmr_config.cpp:228-240). */
@@ -58,6 +61,18 @@ const char *rwnmr_last_error(const rwnmr_ctx *ctx);
 const char *rwnmr_version(void);
 /* Runs subsequent work on an external cudaStream_t (NULL restores the context's own stream). */
 rwnmr_status rwnmr_ctx_set_stream(rwnmr_ctx *ctx, void *cuda_stream);
+
+/* Device allocator of the engine contexts' buffers (images, walkers, tables, accumulators): by
+ * default cudaMalloc / cudaFree; after this call, alloc(bytes, user) / free_fn(ptr, user) for every
+ * allocation made from then on by any context in the process (a buffer is always freed by the
+ * allocator that made it). alloc must return device memory of the context's device, aligned to at
+ * least 256 bytes and usable on the context's stream, or NULL: the call that needed it then fails
+ * with RWNMR_ERR_NOMEM and the context stays usable. Both NULL restores cudaMalloc / cudaFree; one
+ * NULL is RWNMR_ERR_INVALID. For frameworks that own the GPU's memory (a caching allocator) and for
+ * allocation-failure tests. Batch objects allocate with cudaMalloc. */
+typedef void *(*rwnmr_alloc_fn)(size_t bytes, void *user);
+typedef void (*rwnmr_free_fn)(void *ptr, void *user);
+rwnmr_status rwnmr_set_device_allocator(rwnmr_alloc_fn alloc, rwnmr_free_fn free_fn, void *user);
 /* Kernels launched by this context so far (for launch accounting). */
 int64_t rwnmr_ctx_launch_count(const rwnmr_ctx *ctx);
 /* Device-side duration of the last walk kernel(s) of the last run call, in milliseconds. */
@@ -267,6 +282,18 @@ typedef struct rwnmr_batch_cpmg_params
 rwnmr_status rwnmr_batch_create(rwnmr_batch **out, int device);
 void rwnmr_batch_destroy(rwnmr_batch *batch);
 const char *rwnmr_batch_last_error(const rwnmr_batch *batch);
+
+/* Asks the persistent batch walk in flight on batch (or the next one to start) to stop: its CTAs take
+ * no further work items, the kernel ends normally, and the call returns RWNMR_ERR_CANCELLED with no
+ * results (stored histograms are dropped); later calls run normally. Safe to call from another host
+ * thread while a batch call runs. No counterpart in the reference. */
+rwnmr_status rwnmr_batch_cancel(rwnmr_batch *batch);
+
+/* Time budget of each persistent batch walk launch, in seconds (0, the default: none). A CTA that has
+ * run longer than the budget takes no further work items; the call then returns RWNMR_ERR_TIMEOUT
+ * with no results. A bound on how long one walk can hold a shared GPU, not a precise deadline: work
+ * items in progress finish first. */
+rwnmr_status rwnmr_batch_set_time_budget(rwnmr_batch *batch, double seconds);
 double rwnmr_batch_last_kernel_ms(const rwnmr_batch *batch);
 int64_t rwnmr_batch_launch_count(const rwnmr_batch *batch);
 /* Adds one image (bit-blocks as for rwnmr_image_upload) with its walkers; *index = image number. */

@@ -76,6 +76,8 @@ struct BatchLaunch
     const uint64_t *seed0;
     unsigned *counter;
     unsigned *status;
+    const volatile int *cancel;    // mapped host word: nonzero asks the walk to stop taking work
+    unsigned long long budget_ns;  // per-CTA time budget of the walk (0: none)
     unsigned *hist;                // collision histograms (histogram walk), see hist_row
     uint2 *hist_range;             // [image][n_echoes + 1]: first and last non-zero count of each row
 };
@@ -98,6 +100,35 @@ __device__ __forceinline__ DevImage dev_image(const BatchImage &img, int bc)
     im.bc = bc;
     im.shift = 0;
     return im;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The next work item for the calling CTA (thread 0 calls it) -- or none, once the queue is empty,
+// the batch has been cancelled or the CTA has run longer than the time budget since t0. An item
+// taken and then abandoned marks the walk incomplete in the status word; the kernel ends normally,
+// so a stop request never leaves a waiting kernel behind, and a walk that finished every item
+// never reports a stop.
+__device__ __forceinline__ int next_item(const BatchLaunch &L, unsigned long long t0)
+{
+    const int item = (int)atomicAdd(L.counter, 1u);
+    if (item >= L.n_items) return item;
+    if (*L.cancel)
+    {
+        atomicOr(L.status, kStatusCancelled);
+        return L.n_items;
+    }
+    if (L.budget_ns && globaltimer_ns() - t0 > L.budget_ns)
+    {
+        atomicOr(L.status, kStatusBudget);
+        return L.n_items;
+    }
+    return item;
 }
 
 // Loads the walkers of work item w that this thread walks: first + threadIdx.x + j * blockDim.x.
@@ -160,9 +191,10 @@ __global__ void __launch_bounds__(512, 2) batch_cpmg_kernel(BatchLaunch L)
     extern __shared__ unsigned long long sacc[]; // [kWin][kCand][4]
     __shared__ int s_item;
     const int lane = threadIdx.x & 31;
+    const unsigned long long t0 = threadIdx.x == 0 ? globaltimer_ns() : 0;
     for (;;)
     {
-        if (threadIdx.x == 0) s_item = (int)atomicAdd(L.counter, 1u);
+        if (threadIdx.x == 0) s_item = next_item(L, t0);
         __syncthreads();
         const int item = s_item;
         __syncthreads();
@@ -265,9 +297,10 @@ __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
 {
     __shared__ int s_item;
     __shared__ uint4 sdir[6]; // Morton direction table of the current item's image
+    const unsigned long long t0 = threadIdx.x == 0 ? globaltimer_ns() : 0;
     for (;;)
     {
-        if (threadIdx.x == 0) s_item = (int)atomicAdd(L.counter, 1u);
+        if (threadIdx.x == 0) s_item = next_item(L, t0);
         __syncthreads();
         const int item = s_item;
         __syncthreads();
@@ -508,6 +541,9 @@ struct rwnmr_batch
     double *h_f = nullptr;
     unsigned long long *h_acc = nullptr;
     unsigned *h_status = nullptr;
+    int *h_cancel = nullptr;            // mapped pinned word set by rwnmr_batch_cancel
+    const int *d_cancel = nullptr;      // its device address
+    unsigned long long budget_ns = 0;   // rwnmr_batch_set_time_budget
     cudaGraphExec_t graph = nullptr;
     int graph_key[7] = {0, 0, 0, 0, 0, 0, 0};
     // per-echo collision histograms of the last histogram walk, valid for hist_key
@@ -702,6 +738,8 @@ BatchLaunch launch_args(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
     L.seed0 = b->d_seed;
     L.counter = b->d_counter;
     L.status = b->d_status;
+    L.cancel = b->d_cancel;
+    L.budget_ns = b->budget_ns;
     L.hist = b->d_hist;
     L.hist_range = b->d_hist_range;
     return L;
@@ -783,6 +821,25 @@ int resolve_method(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
 
 // Runs the histogram walk unless the stored histograms already belong to this walk (same echoes,
 // steps per echo and boundary condition; images and walkers are fixed once uploaded).
+// The status word of the last persistent walk: a walker outside its image, or a walk stopped by
+// rwnmr_batch_cancel or the time budget (its sums are incomplete; a cancel request is consumed).
+rwnmr_status walk_status(rwnmr_batch *b)
+{
+    const unsigned st = *b->h_status;
+    if (st & (kStatusCancelled | kStatusBudget))
+    {
+        b->hist_valid = false;
+        if (st & kStatusCancelled)
+        {
+            __atomic_store_n(b->h_cancel, 0, __ATOMIC_SEQ_CST);
+            return put(b->err, RWNMR_ERR_CANCELLED, "batch walk cancelled");
+        }
+        return put(b->err, RWNMR_ERR_TIMEOUT, "batch walk exceeded its time budget of %g s", b->budget_ns * 1e-9);
+    }
+    if (st & kStatusBadStart) return put(b->err, RWNMR_ERR_INVALID, "a walker starts outside its image");
+    return RWNMR_OK;
+}
+
 rwnmr_status histogram_walk(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, int block, int wpt, bool force,
                             bool *walked)
 {
@@ -834,7 +891,7 @@ rwnmr_status histogram_walk(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, in
     float ms = 0.f;
     cudaEventElapsedTime(&ms, b->ev0, b->ev1);
     b->hist_ms = ms;
-    if (*b->h_status & kStatusBadStart) return put(b->err, RWNMR_ERR_INVALID, "a walker starts outside its image");
+    if (rwnmr_status ws = walk_status(b)) return ws;
     b->hist_key[0] = p->n_echoes;
     b->hist_key[1] = p->steps_per_echo;
     b->hist_key[2] = p->bc;
@@ -874,12 +931,17 @@ rwnmr_status rwnmr_batch_create(rwnmr_batch **out, int device)
     rwnmr_batch *b = new rwnmr_batch();
     b->device = device;
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
+    void *dc = nullptr;
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+        cudaHostAlloc((void **)&b->h_cancel, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(&dc, b->h_cancel, 0) != cudaSuccess)
     {
         rwnmr_batch_destroy(b);
         return RWNMR_ERR_CUDA;
     }
+    *b->h_cancel = 0;
+    b->d_cancel = (const int *)dc;
     *out = b;
     return RWNMR_OK;
 }
@@ -894,7 +956,25 @@ void rwnmr_batch_destroy(rwnmr_batch *b)
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->h_cancel) cudaFreeHost(b->h_cancel);
     delete b;
+}
+
+rwnmr_status rwnmr_batch_cancel(rwnmr_batch *b)
+{
+    if (!b || !b->h_cancel) return RWNMR_ERR_INVALID;
+    __atomic_store_n(b->h_cancel, 1, __ATOMIC_SEQ_CST);
+    return RWNMR_OK;
+}
+
+rwnmr_status rwnmr_batch_set_time_budget(rwnmr_batch *b, double seconds)
+{
+    if (!b) return RWNMR_ERR_INVALID;
+    if (!(seconds >= 0.0) || seconds > 1.0e6) return put(b->err, RWNMR_ERR_INVALID, "time budget %g s", seconds);
+    b->budget_ns = (unsigned long long)(seconds * 1e9);
+    if (b->graph) cudaGraphExecDestroy(b->graph); // the budget is a captured launch parameter
+    b->graph = nullptr;
+    return RWNMR_OK;
 }
 
 const char *rwnmr_batch_last_error(const rwnmr_batch *b) { return b ? b->err.c_str() : "null batch"; }
@@ -1005,7 +1085,7 @@ rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, 
     cudaEventElapsedTime(&ms, b->ev0, b->ev1);
     b->last_ms = ms + walk_ms; // this call's GPU time, its histogram walk included
     b->last_eval_ms = hist ? ms : 0.0;
-    if (*b->h_status & kStatusBadStart) return put(b->err, RWNMR_ERR_INVALID, "a walker starts outside its image");
+    if (rwnmr_status ws = walk_status(b)) return ws;
     const int E1 = p->n_echoes + 1;
     for (int k = 0; k < ni; k++)
     {

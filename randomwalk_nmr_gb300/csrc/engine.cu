@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -19,26 +20,63 @@ namespace
 {
 typedef unsigned __int128 u128;
 
+// Device allocator of the engine contexts' buffers: cudaMalloc / cudaFree, or the caller's pair set by
+// rwnmr_set_device_allocator (for example a framework's caching allocator).
+struct AllocHook
+{
+    rwnmr_alloc_fn alloc = nullptr;
+    rwnmr_free_fn free = nullptr;
+    void *user = nullptr;
+};
+std::mutex g_alloc_mu;
+AllocHook g_alloc;
+
+AllocHook current_alloc()
+{
+    std::lock_guard<std::mutex> lock(g_alloc_mu);
+    return g_alloc;
+}
+
 template <typename T>
 struct DevBuf
 {
     T *p = nullptr;
     size_t cap = 0;
+    AllocHook hook; // the allocator that made p, which also frees it
     cudaError_t ensure(size_t n)
     {
         if (n <= cap && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMalloc((void **)&p, std::max<size_t>(n, 1) * sizeof(T));
-        if (e == cudaSuccess) cap = std::max<size_t>(n, 1);
-        return e;
+        release();
+        const size_t count = std::max<size_t>(n, 1);
+        const AllocHook h = current_alloc();
+        if (h.alloc)
+        {
+            p = (T *)h.alloc(count * sizeof(T), h.user);
+            if (!p) return cudaErrorMemoryAllocation;
+        }
+        else
+        {
+            cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+            if (e != cudaSuccess)
+            {
+                p = nullptr;
+                return e;
+            }
+        }
+        hook = h;
+        cap = count;
+        return cudaSuccess;
     }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p)
+        {
+            if (hook.alloc) hook.free(p, hook.user);
+            else cudaFree(p);
+        }
         p = nullptr;
         cap = 0;
+        hook = AllocHook{};
     }
 };
 
@@ -307,6 +345,16 @@ rwnmr_status rwnmr_ctx_set_stream(rwnmr_ctx *c, void *s)
 
 int64_t rwnmr_ctx_launch_count(const rwnmr_ctx *c) { return c ? c->launches : 0; }
 double rwnmr_ctx_last_kernel_ms(const rwnmr_ctx *c) { return c ? c->last_ms : 0.0; }
+
+rwnmr_status rwnmr_set_device_allocator(rwnmr_alloc_fn alloc, rwnmr_free_fn free_fn, void *user)
+{
+    if ((alloc == nullptr) != (free_fn == nullptr)) return RWNMR_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(g_alloc_mu);
+    g_alloc.alloc = alloc;
+    g_alloc.free = free_fn;
+    g_alloc.user = alloc ? user : nullptr;
+    return RWNMR_OK;
+}
 
 // ---- image ------------------------------------------------------------------------------------
 static rwnmr_status set_dims(rwnmr_ctx *c, int32_t nx, int32_t ny, int32_t nz, int32_t n_phases)

@@ -16,6 +16,8 @@ constexpr int kDirectMaxG = 128; // gradient points handled by the general-direc
 constexpr unsigned kStatusBadStart = 1u;  // a walker started outside the image (noflux)
 constexpr unsigned kStatusHistRange = 2u; // a displacement fell outside the histogram
 constexpr unsigned kStatusBadLabel = 4u;  // a label exceeded the supported phase count
+constexpr unsigned kStatusCancelled = 8u; // a persistent batch walk stopped taking work: cancelled
+constexpr unsigned kStatusBudget = 16u;   // a persistent batch walk stopped taking work: time budget spent
 
 // Walker state, structure of arrays. coll is [n_phases][n].
 struct WalkState

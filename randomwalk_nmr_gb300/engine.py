@@ -27,6 +27,8 @@ STATUS = {
     4: "RWNMR_ERR_STATE",
     5: "RWNMR_ERR_UNSUPPORTED",
     6: "RWNMR_ERR_DEVICE",
+    7: "RWNMR_ERR_CANCELLED",
+    8: "RWNMR_ERR_TIMEOUT",
 }
 
 # Every function the C header declares, for load checks.
@@ -36,6 +38,7 @@ EXPORTS = [
     "rwnmr_image_download_blocks", "rwnmr_image_layout", "rwnmr_ctx_set_image_layout", "rwnmr_walkers_upload", "rwnmr_walkers_download", "rwnmr_cpmg_run",
     "rwnmr_cpmg_run_sens", "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_map_continue", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
     "rwnmr_cpmg_run_noalloc", "rwnmr_batch_create", "rwnmr_batch_destroy", "rwnmr_batch_last_error",
+    "rwnmr_batch_cancel", "rwnmr_batch_set_time_budget", "rwnmr_set_device_allocator",
     "rwnmr_batch_last_kernel_ms", "rwnmr_batch_launch_count", "rwnmr_batch_add_image", "rwnmr_batch_cpmg",
     "rwnmr_batch_autotune", "rwnmr_batch_collision_histogram", "rwnmr_batch_histogram_walk_ms",
     "rwnmr_field_set_uniform", "rwnmr_field_upload", "rwnmr_field_clear",
@@ -76,6 +79,37 @@ class PfgseParams(ctypes.Structure):
 
 def library_path() -> str:
     return _build.LIB
+
+
+_ALLOC_FN = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p)
+_FREE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p)
+_ALLOC_KEEP = []  # every callback pair ever installed: buffers are freed by the allocator that made them
+
+
+def set_device_allocator(alloc=None, free=None):
+    """Route the engine contexts' device allocations through alloc(nbytes) -> device pointer (int;
+    0 when it cannot allocate, which the calls report as RWNMR_ERR_NOMEM) and free(pointer).
+    Both None restores cudaMalloc / cudaFree. Affects allocations made after the call."""
+    lib = load_library()
+    if alloc is None and free is None:
+        st = lib.rwnmr_set_device_allocator(None, None, None)
+    elif alloc is None or free is None:
+        raise ValueError("give both alloc and free, or neither")
+    else:
+        a = _ALLOC_FN(lambda n, user: alloc(int(n)) or None)
+        f = _FREE_FN(lambda ptr, user: free(int(ptr)))
+        _ALLOC_KEEP.append((a, f))
+        st = lib.rwnmr_set_device_allocator(a, f, None)
+    if st != 0:
+        raise RwnmrError(st, "rwnmr_set_device_allocator")
+
+
+def use_torch_allocator(device: int = 0):
+    """Allocate the engine contexts' device buffers from PyTorch's caching allocator."""
+    import torch
+
+    set_device_allocator(lambda n: torch.cuda.caching_allocator_alloc(n, device),
+                         lambda ptr: torch.cuda.caching_allocator_delete(ptr))
 
 
 def load_library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -366,6 +400,16 @@ class Batch:
     def _check(self, st):
         if st != 0:
             raise RwnmrError(st, self.lib.rwnmr_batch_last_error(self.b).decode())
+
+    def cancel(self):
+        """Stop the batch walk in flight (or the next one): it raises RWNMR_ERR_CANCELLED. Callable from
+        another thread while a batch call runs."""
+        self._check(self.lib.rwnmr_batch_cancel(self.b))
+
+    def set_time_budget(self, seconds: float):
+        """Bound each persistent batch walk to about `seconds` (0: no bound); a walk that runs out
+        raises RWNMR_ERR_TIMEOUT."""
+        self._check(self.lib.rwnmr_batch_set_time_budget(self.b, ctypes.c_double(seconds)))
 
     def add_image(self, blocks, shape, x0, y0, z0, seed0) -> int:
         blocks = np.ascontiguousarray(blocks, np.uint64)

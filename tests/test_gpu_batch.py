@@ -120,3 +120,44 @@ def test_collision_histograms_match_oracle(oracle):
     with pytest.raises(Exception):
         b.collision_histogram(0, n_echoes + 1)
     b.close()
+
+
+def _big_batch():
+    """Four images with 200k walkers each: more work items than resident CTAs."""
+    b = Batch(0)
+    for k in range(4):
+        lab, _ = host.synth_spheres((48, 44, 40), 2.0, 6.0, 0.35, 1, seed=300 + k)
+        blocks, _ = host.pack_blocks(lab)
+        w = host.place_walkers(blocks, lab.shape, 200_000, 700 + k)[:4]
+        b.add_image(blocks, lab.shape, *w)
+    return b
+
+
+@pytest.mark.parametrize("method", ["walk", "histograms"])
+def test_batch_cancel_and_time_budget(method):
+    """A cancelled walk and a walk past its time budget stop taking work items, end normally and
+    raise RWNMR_ERR_CANCELLED / RWNMR_ERR_TIMEOUT; the batch then runs normally and gives the same
+    sums as a batch that was never stopped."""
+    from randomwalk_nmr_gb300 import RwnmrError
+    f = dfactor(np.linspace(2.0, 50.0, 16))[None, :].repeat(4, axis=0)
+    ref_b = _big_batch()
+    ref = ref_b.cpmg(f, 40, 3, method=method)
+    ref_b.close()
+    b = _big_batch()
+    b.cancel()
+    with pytest.raises(RwnmrError) as e:
+        b.cpmg(f, 40, 3, method=method)
+    assert e.value.status == 7
+    got = b.cpmg(f, 40, 3, method=method)  # the request was consumed
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    b.set_time_budget(1e-9)
+    with pytest.raises(RwnmrError) as e:
+        b.cpmg(f, 40, 3, method="walk")  # walks again whatever the stored histograms
+    assert e.value.status == 8
+    b.set_time_budget(0.0)
+    got = b.cpmg(f, 40, 3, method=method)
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    b.set_time_budget(60.0)  # a generous budget changes nothing
+    got = b.cpmg(f, 40, 3, method=method)
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    b.close()

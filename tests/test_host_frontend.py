@@ -204,3 +204,14 @@ def test_cli_reports_missing_config_without_gpu(tmp_path):
     rc = host.cli(["--config-root", str(tmp_path), "-rwconfig", str(tmp_path / "missing.config"), "cpmg"],
                   cwd=str(tmp_path))
     assert rc == 1
+
+
+def test_placement_in_an_image_without_pores_is_an_error():
+    import numpy as np
+
+    from randomwalk_nmr_gb300 import host
+
+    lab = np.ones((8, 8, 8), np.uint8)
+    blocks, _ = host.pack_blocks(lab)
+    with pytest.raises(ValueError, match="placement failed"):
+        host.place_walkers(blocks, lab.shape, 10, 1)
