@@ -18,7 +18,7 @@ Reported:
              sample with all host threads
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload NAME]
-  workloads: cpmg-2phase-400 (default), cpmg-1phase-100, cpmg-2phase-small, pfgse-256[-small],
+  workloads: cpmg-2phase-400 (default), cpmg-1phase-100, cpmg-2phase-small, map-400, pfgse-256[-small],
              rho-fit-multiphase[-small], rho-fit-batch[-small]
 """
 from __future__ import annotations
@@ -42,6 +42,12 @@ FALLBACK_HBM_GBS = 6800.0
 
 
 def workload(name: str):
+    if name == "map-400":
+        # the reference's collision-mapping walk (mapSimulation) on the headline image and walkers:
+        # 20,000 steps, per-walker collision counts out
+        w = workload("cpmg-2phase-400")
+        w.update(name=name, map=True)
+        return w
     if name == "cpmg-2phase-400":
         return dict(name=name, shape=(400, 400, 400), rmin=6.0, rmax=20.0, porosity=0.25, n_phases=2, img_seed=2,
                     walkers=1_000_000, seed=7, rho=[5.0, 25.0], d0=2.5, te=0.1, echoes=20_000, bc="noflux")
@@ -570,7 +576,12 @@ def main():
     gamma = 1.0e6 * 42.576 * 2.0 * np.pi
     dt_s = 1.0e-3 * res * res / (6.0 * w["d0"])
 
+    mapping = bool(w.get("map"))
+
     def walk():
+        if mapping:
+            coll = eng.map(w["echoes"] * spe, bc=w["bc"])
+            return dict(echo_sum=None, echo_fx=coll)
         if field:
             o = eng.cpmg_field(w["echoes"], spe, f, gamma, dt_s, bc=w["bc"])
             return dict(echo_sum=o["echo_sum"], echo_fx=o["echo_sum"], phase=o["phase"])
@@ -595,7 +606,7 @@ def main():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    if dist and not field:
+    if dist and not field and not mapping:
         from randomwalk_nmr_gb300.shard import combine_cpmg
 
         out = combine_cpmg(out)  # the whole population's echo train on every rank
@@ -622,7 +633,7 @@ def main():
             if field:
                 eng.set_field_uniform(field[0], field[1], res)
             o2 = walk()
-            if dist and not field:
+            if dist and not field and not mapping:
                 o2 = combine_cpmg(o2)
             t1 = time.perf_counter()
             if k:
@@ -632,6 +643,8 @@ def main():
         d2h = (w["echoes"] + 1) * (3 + (1 if w["n_phases"] == 1 else (2 if w["n_phases"] == 2 else 4))) * 8 + 4
         if field:
             d2h = (w["echoes"] + 1) * 3 * 8 + 4 + n * 8  # echo limbs, status, final phases
+        if mapping:
+            d2h = n * 4 + 4  # per-walker collision counts, status
         te = statistics.mean(e2e_s)
         if dist:
             tt = torch.tensor([te], device=f"cuda:{local}")
@@ -704,6 +717,18 @@ def main():
         sub.close()
         echo_err = float(np.max(np.abs(og["echo_sum"] - ob["echo_fp64"])) / m)
         assert np.array_equal(og["phase"].view(np.uint64), ob["phasef"].view(np.uint64)), "phases differ from the oracle"
+    elif rank == 0 and not args.no_cpu_baseline and mapping:
+        # the CPU walk of the oracle (the mapping walk's steps plus the energy update) on a sample;
+        # the GPU mapping walk's per-walker collision counts on that sample must equal the oracle's
+        base, ob, sample = cpu_baseline(labels, w["n_phases"], walkers, spe, w["echoes"], f, w["bc"])
+        sub = Engine(local)
+        sub.upload_labels(labels, w["n_phases"])
+        sub.upload_walkers(*sample)
+        cm = sub.map(w["echoes"] * spe, bc=w["bc"])
+        sub.close()
+        assert np.array_equal(cm, np.asarray(ob["collf"]).reshape(len(cm), -1).sum(axis=1)), \
+            "collision counts differ from the oracle"
+        echo_err = 0.0
     elif rank == 0 and not args.no_cpu_baseline:
         base, ob, sample = cpu_baseline(labels, w["n_phases"], walkers, spe, w["echoes"], f, w["bc"])
         # echo error of the GPU walk against the FP64 oracle on the same walker sample
@@ -716,11 +741,13 @@ def main():
         assert np.array_equal(og["echo_coll"], ob["echo_coll"]), "per-echo collision counts differ from the oracle"
 
     if rank == 0:
-        line = {"metric": "walker-steps/s (CPMG in an internal field)" if field else "walker-steps/s (plain CPMG)",
+        line = {"metric": ("walker-steps/s (collision-mapping walk)" if mapping else
+                           "walker-steps/s (CPMG in an internal field)" if field else "walker-steps/s (plain CPMG)"),
                 "value": value, "unit": "walker-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": t_step * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "int32/u64 walk, exact 64-bit fixed-point echo sums, f64 output",
+                "dtype": ("int32/u64 walk, u32 collision counts" if mapping else
+                          "int32/u64 walk, exact 64-bit fixed-point echo sums, f64 output"),
                 "data": "synthetic sphere pack (no reference benchmark data)",
                 "config": {"workload": w["name"], "image": "x".join(map(str, w["shape"])), "porosity": round(por, 4),
                            "phases": w["n_phases"], "walkers": n, "echoes": w["echoes"], "steps_per_echo": spe,
@@ -729,9 +756,11 @@ def main():
                            "parallelism": (f"walkers sharded over {world} GPUs ({n} per GPU), exact integer "
                                            "all-reduce of the echo limb sums") if world > 1 else "1 GPU"},
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches),
-                ("echo_max_abs_err_per_walker_vs_oracle" if field else "echo_max_rel_err_vs_fp64_oracle"): echo_err,
-                "clocks": clk_sum,
-                "echo_check": float(out["echo_sum"][-1] / out["echo_sum"][0])}
+                ("collision_counts_max_abs_diff_vs_oracle" if mapping else
+                 "echo_max_abs_err_per_walker_vs_oracle" if field else "echo_max_rel_err_vs_fp64_oracle"): echo_err,
+                "clocks": clk_sum}
+        if not mapping:
+            line["echo_check"] = float(out["echo_sum"][-1] / out["echo_sum"][0])
         print(json.dumps(line))
     eng.close()
     if dist:
