@@ -142,6 +142,10 @@ struct rwnmr_ctx
     DevBuf<uint64_t> seed0, seed;
     DevBuf<uint32_t> coll;
     DevBuf<int32_t> rx, ry, rz; // scratch walker state of the adjoint's sensitivity walk
+    DevBuf<int32_t> sperm, ti32; // walker re-sort: the new order and per-type scratch
+    DevBuf<uint64_t> tu64;
+    DevBuf<uint32_t> tu32;
+    DevBuf<double> tf64;
     DevBuf<uint64_t> rseed;
     DevBuf<uint32_t> rcoll;
 
@@ -328,6 +332,7 @@ void rwnmr_ctx_destroy(rwnmr_ctx *c)
     c->gbuf.release(); c->ibuf.release(); c->disp.release(); c->energy.release();
     c->wf.release(); c->wenergy.release(); c->field.release(); c->phase.release(); c->btab.release();
     c->rx.release(); c->ry.release(); c->rz.release(); c->rseed.release(); c->rcoll.release();
+    c->sperm.release(); c->ti32.release(); c->tu64.release(); c->tu32.release(); c->tf64.release();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -956,6 +961,51 @@ rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const 
 static rwnmr_status map_impl(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions,
                              bool from_initial);
 
+constexpr int64_t kMapResortSteps = 2048; // steps per launch of a re-sorted mapping walk
+
+// Re-sorts the stored walkers by their current positions -- the upload-time order by start position
+// loses its locality as a long walk spreads them: every persistent per-walker array is permuted
+// alike and the stored-to-upload permutation is composed, so all outputs still come back in upload
+// order.
+static rwnmr_status reorder_walkers(rwnmr_ctx *c, int shift)
+{
+    const int64_t n = c->n;
+    if (n <= 1) return RWNMR_OK;
+    const size_t n1 = (size_t)n;
+    const int slots = phase_slots(c->n_phases);
+    RW_CUDA(c, c->sperm.ensure(n1), "walker reorder");
+    RW_CUDA(c, walker_order(c->x.p, c->y.p, c->z.p, n, shift, c->order_scratch.p, c->sperm.p, c->stream),
+            "walker reorder");
+    RW_CUDA(c, c->ti32.ensure(n1), "walker reorder");
+    for (DevBuf<int32_t> *a : {&c->x0, &c->y0, &c->z0, &c->x, &c->y, &c->z, &c->perm})
+    {
+        RW_CUDA(c, permute_u32(c->sperm.p, n, (const uint32_t *)a->p, (uint32_t *)c->ti32.p, c->stream), "walker reorder");
+        std::swap(*a, c->ti32);
+        RW_CUDA(c, c->ti32.ensure(n1), "walker reorder");
+    }
+    RW_CUDA(c, c->tu64.ensure(n1), "walker reorder");
+    for (DevBuf<uint64_t> *a : {&c->seed0, &c->seed})
+    {
+        RW_CUDA(c, permute_u64(c->sperm.p, n, a->p, c->tu64.p, c->stream), "walker reorder");
+        std::swap(*a, c->tu64);
+        RW_CUDA(c, c->tu64.ensure(n1), "walker reorder");
+    }
+    RW_CUDA(c, c->tu32.ensure(n1 * slots), "walker reorder");
+    for (int q = 0; q < slots; q++)
+        RW_CUDA(c, permute_u32(c->sperm.p, n, c->coll.p + q * n1, c->tu32.p + q * n1, c->stream), "walker reorder");
+    std::swap(c->coll, c->tu32);
+    if (c->has_wf)
+    {
+        RW_CUDA(c, c->tf64.ensure(n1), "walker reorder");
+        RW_CUDA(c, permute_u64(c->sperm.p, n, (const uint64_t *)c->wf.p, (uint64_t *)c->tf64.p, c->stream),
+                "walker reorder");
+        std::swap(c->wf, c->tf64);
+    }
+    c->h_perm_valid = false;
+    c->launches += 7 + 9 + slots + (c->has_wf ? 1 : 0); // the sort's 7 kernels, one per permuted array
+    return RWNMR_OK;
+}
+
 rwnmr_status rwnmr_map_run(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions)
 {
     return map_impl(c, bc, shift, steps, collisions, true);
@@ -980,8 +1030,11 @@ static rwnmr_status map_impl(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t st
     L.status = c->status.p;
     L.tstride = 1;
     const DevImage im = c->image(bc, shift);
-    const WalkState st = c->state();
-    const int64_t chunk = 1 << 14;
+    WalkState st = c->state();
+    // long walks of many walkers: shorter launches with the walkers re-sorted by position between
+    // them, so a warp's gathers keep sharing cache lines (the sorted start order fades as they spread)
+    const bool resort = c->n >= (1 << 16) && steps > 2 * kMapResortSteps;
+    const int64_t chunk = resort ? kMapResortSteps : (1 << 14);
     RW_CUDA(c, cudaEventRecord(c->ev0, c->stream), "event");
     if (c->n > 0)
     {
@@ -996,6 +1049,11 @@ static rwnmr_status map_impl(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t st
         }
         for (int64_t s = 0; s < steps; s += chunk)
         {
+            if (resort && s > 0)
+            {
+                RW_TRY(reorder_walkers(c, shift));
+                st = c->state();
+            }
             L.e_begin = 0;
             L.e_end = 1;
             L.steps_per_echo = (int)std::min<int64_t>(chunk, steps - s);

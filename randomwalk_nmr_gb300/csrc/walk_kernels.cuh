@@ -136,6 +136,9 @@ cudaError_t launch_pfgse_direct(const DirectLaunch &L, int n_delta, int blocks, 
 size_t walker_order_scratch_words(int64_t n);
 cudaError_t walker_order(const int32_t *x, const int32_t *y, const int32_t *z, int64_t n, int shift, uint32_t *scratch,
                          int32_t *perm, cudaStream_t s);
+// dst[k] = src[perm[k]], k < n
+cudaError_t permute_u32(const int32_t *perm, int64_t n, const uint32_t *src, uint32_t *dst, cudaStream_t s);
+cudaError_t permute_u64(const int32_t *perm, int64_t n, const uint64_t *src, uint64_t *dst, cudaStream_t s);
 // x0[k] = ux[perm[k]] (and y, z, seeds)
 cudaError_t gather_walkers(const int32_t *perm, int64_t n, const int32_t *ux, const int32_t *uy, const int32_t *uz,
                            const uint64_t *us, int32_t *x0, int32_t *y0, int32_t *z0, uint64_t *s0, cudaStream_t s);

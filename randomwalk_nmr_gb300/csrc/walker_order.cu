@@ -176,6 +176,30 @@ cudaError_t walker_order(const int32_t *x, const int32_t *y, const int32_t *z, i
     return cudaGetLastError();
 }
 
+namespace
+{
+template <typename T>
+__global__ void permute_kernel(const int32_t *__restrict__ perm, int64_t n, const T *__restrict__ src, T *__restrict__ dst)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = src[perm[k]];
+}
+} // namespace
+
+cudaError_t permute_u32(const int32_t *perm, int64_t n, const uint32_t *src, uint32_t *dst, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    permute_kernel<uint32_t><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(perm, n, src, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t permute_u64(const int32_t *perm, int64_t n, const uint64_t *src, uint64_t *dst, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    permute_kernel<uint64_t><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(perm, n, src, dst);
+    return cudaGetLastError();
+}
+
 cudaError_t gather_walkers(const int32_t *perm, int64_t n, const int32_t *ux, const int32_t *uy, const int32_t *uz,
                            const uint64_t *us, int32_t *x0, int32_t *y0, int32_t *z0, uint64_t *s0, cudaStream_t s)
 {

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from conftest import dfactor
-from randomwalk_nmr_gb300 import fx_to_float, host
+from randomwalk_nmr_gb300 import Engine, fx_to_float, host
 
 pytestmark = pytest.mark.gpu
 
@@ -252,3 +252,33 @@ def test_cpmg_morton_and_block_layouts(engine, oracle, shape, n_phases):
                 assert_parity(g, st, o)
     finally:
         engine.allow_morton(True)
+
+
+def test_long_mapping_walk_with_walker_resorting(engine, oracle):
+    """A mapping walk of many walkers (>= 2^16) over more than two 2048-step launches re-sorts the
+    stored walkers by position between launches: collision counts, final positions and seeds still
+    come back in upload order and equal the oracle's, and later walks on the context are unchanged."""
+    lab, _ = host.synth_spheres((40, 36, 44), 2.0, 6.0, 0.35, 2, seed=21)
+    blocks, _ = host.pack_blocks(lab)
+    w = host.place_walkers(blocks, lab.shape, 70_000, 9)[:4]
+    engine.upload_labels(lab, 2)
+    engine.upload_walkers(*w)
+    steps = 5000
+    coll = engine.map(steps)
+    st = engine.download_walkers()
+    m = 3000
+    sub = tuple(a[:m] for a in w)
+    f = dfactor([10.0, 30.0])
+    o = oracle.cpmg(lab, sub, 1, steps, f, n_phases=2, threads=4)
+    assert np.array_equal(coll[:m], o["collf"].sum(axis=1))
+    assert np.array_equal(st["x"][:m], o["xf"]) and np.array_equal(st["y"][:m], o["yf"])
+    assert np.array_equal(st["z"][:m], o["zf"]) and np.array_equal(st["seed"][:m], o["seedf"])
+    assert np.array_equal(st["collisions"][:m], o["collf"])
+    # the re-sorted context walks from the same initial state as a fresh one
+    a = engine.cpmg(60, 2, f)["echo_fx"]
+    fresh = Engine(0)
+    fresh.upload_labels(lab, 2)
+    fresh.upload_walkers(*w)
+    b = fresh.cpmg(60, 2, f)["echo_fx"]
+    fresh.close()
+    assert np.array_equal(a, b)
