@@ -9,6 +9,7 @@
 // order inside each tile (warp match ranks plus per-warp digit counts). Stability makes the
 // permutation a function of the positions alone, so FP64 block sums that follow walker order (the
 // adjoint, the general-direction PFGSE path) stay reproducible.
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -21,6 +22,7 @@ namespace
 constexpr int kSortThreads = 256;
 constexpr int kSortChunks = 16;
 constexpr int kSortTile = kSortThreads * kSortChunks; // elements per tile
+constexpr int kScanBlocks = 1024;                     // most blocks of the digit-count scan
 constexpr unsigned FULLM = 0xffffffffu;
 
 __device__ __forceinline__ uint32_t spread10(uint32_t v)
@@ -89,6 +91,68 @@ __global__ void scan_kernel(uint32_t *__restrict__ counts, int64_t m)
     }
 }
 
+// Multi-block exclusive scan of the digit counts: per-block sums of consecutive segments, the
+// scan of those sums (scan_kernel), then each block scans its segment in coalesced rounds of
+// blockDim.x elements from its offset.
+__global__ void scan_reduce_kernel(const uint32_t *__restrict__ counts, int64_t m, int64_t seg,
+                                   uint32_t *__restrict__ sums)
+{
+    __shared__ uint32_t red[32];
+    const int64_t b0 = (int64_t)blockIdx.x * seg, e = b0 + seg < m ? b0 + seg : m;
+    uint32_t v = 0;
+    for (int64_t k = b0 + threadIdx.x; k < e; k += blockDim.x) v += counts[k];
+    v = __reduce_add_sync(FULLM, v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32)
+    {
+        uint32_t t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0u;
+        t = __reduce_add_sync(FULLM, t);
+        if (threadIdx.x == 0) sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void scan_apply_kernel(uint32_t *__restrict__ counts, int64_t m, int64_t seg,
+                                  const uint32_t *__restrict__ offsets)
+{
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) carry = offsets[blockIdx.x];
+    __syncthreads();
+    const int64_t b0 = (int64_t)blockIdx.x * seg, e = b0 + seg < m ? b0 + seg : m;
+    for (int64_t base = b0; base < e; base += blockDim.x)
+    {
+        const int64_t k = base + threadIdx.x;
+        const uint32_t v = k < e ? counts[k] : 0u;
+        uint32_t x = v; // inclusive scan within the warp
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t y = __shfl_up_sync(FULLM, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0)
+        {
+            const uint32_t t = lane < nw ? wsum[lane] : 0u;
+            uint32_t ti = t;
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const uint32_t y = __shfl_up_sync(FULLM, ti, o);
+                if (lane >= o) ti += y;
+            }
+            if (lane < nw) wsum[lane] = ti - t; // warps before this one
+        }
+        __syncthreads();
+        const uint32_t c0 = carry;
+        if (k < e) counts[k] = c0 + wsum[warp] + x - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = c0 + wsum[warp] + x;
+        __syncthreads();
+    }
+}
+
 // Stable scatter of one tile: element order inside the tile is kept for equal digits.
 __global__ void digit_scatter_kernel(const uint32_t *__restrict__ key_in, const int32_t *__restrict__ idx_in,
                                      int64_t n, int pass, int tiles, const uint32_t *__restrict__ offsets,
@@ -148,7 +212,7 @@ __global__ void gather_walkers_kernel(const int32_t *__restrict__ perm, int64_t 
 size_t walker_order_scratch_words(int64_t n)
 {
     const int64_t tiles = (n + kSortTile - 1) / kSortTile;
-    return (size_t)(4 * n + 256 * tiles);
+    return (size_t)(4 * n + 256 * tiles + kScanBlocks);
 }
 
 cudaError_t walker_order(const int32_t *x, const int32_t *y, const int32_t *z, int64_t n, int shift, uint32_t *scratch,
@@ -160,6 +224,10 @@ cudaError_t walker_order(const int32_t *x, const int32_t *y, const int32_t *z, i
     int32_t *idx_a = reinterpret_cast<int32_t *>(scratch + 2 * n);
     int32_t *idx_b = reinterpret_cast<int32_t *>(scratch + 3 * n);
     uint32_t *counts = scratch + 4 * n;
+    uint32_t *sums = counts + (size_t)256 * tiles; // kScanBlocks words
+    const int64_t m = (int64_t)256 * tiles;
+    const int nb = (int)std::min<int64_t>(kScanBlocks, (m + 2047) / 2048);
+    const int64_t seg = (m + nb - 1) / nb;
     const unsigned grid = (unsigned)((n + 255) / 256);
     order_keys_kernel<<<grid, 256, 0, s>>>(x, y, z, n, shift, key_a, idx_a);
     // pass 0: a -> b, pass 1: b -> (key a, perm)
@@ -170,7 +238,9 @@ cudaError_t walker_order(const int32_t *x, const int32_t *y, const int32_t *z, i
         uint32_t *kout = pass ? key_a : key_b;
         int32_t *iout = pass ? perm : idx_b;
         digit_count_kernel<<<tiles, kSortThreads, 0, s>>>(kin, n, pass, tiles, counts);
-        scan_kernel<<<1, 1024, 0, s>>>(counts, (int64_t)256 * tiles);
+        scan_reduce_kernel<<<nb, 1024, 0, s>>>(counts, m, seg, sums);
+        scan_kernel<<<1, 1024, 0, s>>>(sums, nb);
+        scan_apply_kernel<<<nb, 1024, 0, s>>>(counts, m, seg, sums);
         digit_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(kin, iin, n, pass, tiles, counts, kout, iout);
     }
     return cudaGetLastError();
