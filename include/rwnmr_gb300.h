@@ -110,6 +110,14 @@ rwnmr_status rwnmr_walkers_upload(rwnmr_ctx *ctx, int64_t n, const int32_t *x0, 
  * ([n][n_phases]). Any pointer may be NULL. */
 rwnmr_status rwnmr_walkers_download(rwnmr_ctx *ctx, int32_t *x, int32_t *y, int32_t *z, uint64_t *seed,
                                     uint32_t *collisions);
+/* Checkpoint / resume: sets the current walker state from arrays in the layout rwnmr_walkers_download
+ * returns (upload order; collisions [n][n_phases]) -- typically a checkpoint of an earlier walk of
+ * the same walkers, in this or another process. The initial positions and seeds stay those of
+ * rwnmr_walkers_upload. rwnmr_map_continue then resumes the walk exactly where the checkpoint left
+ * it (a walk is a function of this state alone). No counterpart in the reference, whose walkers
+ * re-derive their state from initialSeed and initialPosition. */
+rwnmr_status rwnmr_walkers_restore(rwnmr_ctx *ctx, const int32_t *x, const int32_t *y, const int32_t *z,
+                                   const uint64_t *seed, const uint32_t *collisions);
 
 /* Per-walker decrease factors [n], each in [0, 1]: the reference's Walker::decreaseFactor when it
  * differs between walkers (RHO_TYPE: sigmoid, where each walker's relaxivity follows from its

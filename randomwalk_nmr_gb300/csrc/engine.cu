@@ -551,6 +551,39 @@ rwnmr_status rwnmr_walkers_upload(rwnmr_ctx *c, int64_t n, const int32_t *x0, co
     return RWNMR_OK;
 }
 
+rwnmr_status rwnmr_walkers_restore(rwnmr_ctx *c, const int32_t *x, const int32_t *y, const int32_t *z,
+                                   const uint64_t *seed, const uint32_t *coll)
+{
+    if (!c) return RWNMR_ERR_INVALID;
+    if (!c->has_walkers) return c->fail(RWNMR_ERR_STATE, "no walkers uploaded");
+    const int64_t n = c->n;
+    if (n == 0) return RWNMR_OK;
+    if (!x || !y || !z || !seed || !coll) return c->fail(RWNMR_ERR_INVALID, "NULL walker state");
+    RW_TRY(host_perm(c));
+    const std::vector<int32_t> &pm = c->h_perm;
+    const int P = c->n_phases, slots = phase_slots(P);
+    std::vector<int32_t> tx((size_t)n), ty((size_t)n), tz((size_t)n);
+    std::vector<uint64_t> ts((size_t)n);
+    std::vector<uint32_t> tc((size_t)n * slots, 0u);
+    for (int64_t k = 0; k < n; k++) // to the stored order
+    {
+        const size_t u = (size_t)pm[(size_t)k];
+        tx[(size_t)k] = x[u];
+        ty[(size_t)k] = y[u];
+        tz[(size_t)k] = z[u];
+        ts[(size_t)k] = seed[u];
+        for (int q = 0; q < P; q++) tc[(size_t)q * n + k] = coll[u * P + q];
+    }
+    const size_t b4 = (size_t)n * 4;
+    RW_CUDA(c, cudaMemcpyAsync(c->x.p, tx.data(), b4, cudaMemcpyHostToDevice, c->stream), "walkers restore");
+    RW_CUDA(c, cudaMemcpyAsync(c->y.p, ty.data(), b4, cudaMemcpyHostToDevice, c->stream), "walkers restore");
+    RW_CUDA(c, cudaMemcpyAsync(c->z.p, tz.data(), b4, cudaMemcpyHostToDevice, c->stream), "walkers restore");
+    RW_CUDA(c, cudaMemcpyAsync(c->seed.p, ts.data(), b4 * 2, cudaMemcpyHostToDevice, c->stream), "walkers restore");
+    RW_CUDA(c, cudaMemcpyAsync(c->coll.p, tc.data(), b4 * slots, cudaMemcpyHostToDevice, c->stream), "walkers restore");
+    RW_CUDA(c, cudaStreamSynchronize(c->stream), "walkers restore");
+    return RWNMR_OK;
+}
+
 rwnmr_status rwnmr_walkers_download(rwnmr_ctx *c, int32_t *x, int32_t *y, int32_t *z, uint64_t *seed, uint32_t *coll)
 {
     if (!c) return RWNMR_ERR_INVALID;

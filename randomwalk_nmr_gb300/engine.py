@@ -38,7 +38,7 @@ EXPORTS = [
     "rwnmr_image_download_blocks", "rwnmr_image_layout", "rwnmr_ctx_set_image_layout", "rwnmr_walkers_upload", "rwnmr_walkers_download", "rwnmr_cpmg_run",
     "rwnmr_cpmg_run_sens", "rwnmr_cpmg_adjoint", "rwnmr_map_run", "rwnmr_map_continue", "rwnmr_pfgse_run", "rwnmr_pfgse_grad_g",
     "rwnmr_cpmg_run_noalloc", "rwnmr_batch_create", "rwnmr_batch_destroy", "rwnmr_batch_last_error",
-    "rwnmr_batch_cancel", "rwnmr_batch_set_time_budget", "rwnmr_set_device_allocator",
+    "rwnmr_batch_cancel", "rwnmr_batch_set_time_budget", "rwnmr_set_device_allocator", "rwnmr_walkers_restore",
     "rwnmr_batch_last_kernel_ms", "rwnmr_batch_launch_count", "rwnmr_batch_add_image", "rwnmr_batch_cpmg",
     "rwnmr_batch_autotune", "rwnmr_batch_collision_histogram", "rwnmr_batch_histogram_walk_ms",
     "rwnmr_field_set_uniform", "rwnmr_field_upload", "rwnmr_field_clear",
@@ -249,6 +249,13 @@ class Engine:
         c = np.zeros((n, P), np.uint32)
         self._check(self.lib.rwnmr_walkers_download(self.ctx, _p(x), _p(y), _p(z), _p(s), _p(c)))
         return dict(x=x, y=y, z=z, seed=s, collisions=c)
+
+    def restore_walkers(self, state):
+        """Checkpoint / resume: set the current walker state from a download_walkers() dict."""
+        x, y, z = (np.ascontiguousarray(state[k], np.int32) for k in ("x", "y", "z"))
+        s = np.ascontiguousarray(state["seed"], np.uint64)
+        c = np.ascontiguousarray(state["collisions"], np.uint32).reshape(self.n, self.n_phases)
+        self._check(self.lib.rwnmr_walkers_restore(self.ctx, _p(x), _p(y), _p(z), _p(s), _p(c)))
 
     def set_walker_dfactor(self, dfactor):
         """Per-walker decrease factors (single-phase images); walks called with dfactor=None use them."""
