@@ -27,6 +27,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/rwnmr_gb300.h"
 #include "walk_device.cuh"
@@ -1029,6 +1030,11 @@ rwnmr_status rwnmr_batch_add_image(rwnmr_batch *b, const uint64_t *blocks, int32
 rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, const double *dfactor, double *echo,
                               double *decho)
 {
+    nvtxRangePushA("rwnmr_batch_cpmg");
+    struct Pop
+    {
+        ~Pop() { nvtxRangePop(); }
+    } pop;
     if (!b) return RWNMR_ERR_INVALID;
     rwnmr_status st = check_params(b, p);
     if (st != RWNMR_OK) return st;

@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 
 #include "../../include/rwnmr_gb300.h"
+#include <nvtx3/nvToolsExt.h>
+
 #include "fixed_cos.cuh"
 #include "walk_kernels.cuh"
 
@@ -19,6 +21,15 @@ using namespace rwnmr;
 namespace
 {
 typedef unsigned __int128 u128;
+
+// NVTX range over one C-ABI call (visible in Nsight Systems / Nsight Compute timelines; inert without a tool).
+struct NvtxRange
+{
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Device allocator of the engine contexts' buffers: cudaMalloc / cudaFree, or the caller's pair set by
 // rwnmr_set_device_allocator (for example a framework's caching allocator).
@@ -510,6 +521,7 @@ rwnmr_status rwnmr_image_download_blocks(rwnmr_ctx *c, uint64_t *out)
 rwnmr_status rwnmr_walkers_upload(rwnmr_ctx *c, int64_t n, const int32_t *x0, const int32_t *y0, const int32_t *z0,
                                   const uint64_t *seed0)
 {
+    NvtxRange nvtx("rwnmr_walkers_upload");
     if (!c) return RWNMR_ERR_INVALID;
     if (n < 0 || n > (1ll << 31) - 1) return c->fail(RWNMR_ERR_INVALID, "walker count %lld out of range", (long long)n);
     if (n > 0 && (!x0 || !y0 || !z0 || !seed0)) return c->fail(RWNMR_ERR_INVALID, "walker arrays must not be NULL");
@@ -650,6 +662,7 @@ namespace
 rwnmr_status cpmg_impl(rwnmr_ctx *c, const rwnmr_cpmg_params *p, bool sens, bool scratch, double *echo_sum,
                        uint64_t *echo_fx, uint64_t *echo_coll, double *echo_sens, uint64_t *echo_sens_fx)
 {
+    NvtxRange nvtx(sens ? "rwnmr_cpmg_run_sens" : "rwnmr_cpmg_run");
     RW_TRY(need_run_state(c));
     if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
     RW_TRY(check_geom(c, p->bc, p->shift));
@@ -806,6 +819,7 @@ rwnmr_status rwnmr_field_clear(rwnmr_ctx *c)
 rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p, double *echo_sum, uint64_t *echo_fx,
                                   double *phase_out)
 {
+    NvtxRange nvtx("rwnmr_cpmg_field_run");
     RW_TRY(need_run_state(c));
     if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
     if (c->field_mode == 0) return c->fail(RWNMR_ERR_STATE, "no internal field set");
@@ -911,6 +925,7 @@ rwnmr_status rwnmr_cpmg_field_run(rwnmr_ctx *c, const rwnmr_field_cpmg_params *p
 
 rwnmr_status rwnmr_cpmg_adjoint(rwnmr_ctx *c, const rwnmr_cpmg_params *p, const double *grad_echo, double *grad_dfactor)
 {
+    NvtxRange nvtx("rwnmr_cpmg_adjoint");
     RW_TRY(need_run_state(c));
     if (!p || !grad_echo || !grad_dfactor) return c->fail(RWNMR_ERR_INVALID, "NULL argument");
     if (!p->dfactor) return c->fail(RWNMR_ERR_UNSUPPORTED, "the adjoint differentiates per-phase decrease factors");
@@ -1052,6 +1067,7 @@ rwnmr_status rwnmr_map_continue(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t
 static rwnmr_status map_impl(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t steps, uint32_t *collisions,
                              bool from_initial)
 {
+    NvtxRange nvtx(from_initial ? "rwnmr_map_run" : "rwnmr_map_continue");
     RW_TRY(need_run_state(c));
     RW_TRY(check_geom(c, bc, shift));
     if (steps < 0 || steps > (1ll << 31) - 1) return c->fail(RWNMR_ERR_INVALID, "bad step count");
@@ -1121,6 +1137,7 @@ static rwnmr_status map_impl(rwnmr_ctx *c, int32_t bc, int32_t shift, int64_t st
 static rwnmr_status pfgse_impl(rwnmr_ctx *c, const rwnmr_pfgse_params *p, double *M, double *esum, uint64_t *msd,
                                bool want_grad, double kscale, const double *dir, double *dMdg)
 {
+    NvtxRange nvtx(want_grad ? "rwnmr_pfgse_grad_g" : "rwnmr_pfgse_run");
     RW_TRY(need_run_state(c));
     if (!p) return c->fail(RWNMR_ERR_INVALID, "params is NULL");
     RW_TRY(check_geom(c, p->bc, p->shift));
