@@ -21,7 +21,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "librwnmr_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "librwnmr_ref.so")
-REF_SRC = "/root/reference/src/backend"
+# Root of a RandomWalk_NMR checkout, given by the caller (build recipe or fixture script) through
+# the environment; without it only the restatement is built.
+REF_ENV = "RWNMR_REFERENCE"
 
 BC = {"noflux": 0, "periodic": 1, "mirror": 2}
 
@@ -32,12 +34,28 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(_vp)
 
 
-def build(with_ref: bool | None = None) -> None:
-    """Builds the restatement, and the reference library when its sources are present."""
+def ref_source_dir(ref_root: str | None = None) -> str | None:
+    """The reference's backend source directory under ``ref_root`` (default: $RWNMR_REFERENCE),
+    or None when no checkout is given or it is absent."""
+    root = ref_root if ref_root is not None else os.environ.get(REF_ENV)
+    if not root:
+        return None
+    src = os.path.join(root, "src", "backend")
+    return src if os.path.isdir(src) else None
+
+
+def build(with_ref: bool | None = None, ref_root: str | None = None) -> None:
+    """Builds the restatement, and the reference library when a reference checkout is given
+    (``ref_root`` or $RWNMR_REFERENCE) and present."""
+    src = ref_source_dir(ref_root)
     if with_ref is None:
-        with_ref = os.path.isdir(REF_SRC)
-    target = "ref" if with_ref else "all"
-    subprocess.run(["make", "-s", "-C", HERE, target, "-j8"], check=True)
+        with_ref = src is not None
+    if with_ref and src is None:
+        raise FileNotFoundError("reference sources not found: set %s to a RandomWalk_NMR checkout" % REF_ENV)
+    cmd = ["make", "-s", "-C", HERE, "ref" if with_ref else "all", "-j8"]
+    if with_ref:
+        cmd.append("REF_SRC=" + src)
+    subprocess.run(cmd, check=True)
 
 
 class OrcImage(ctypes.Structure):
@@ -89,6 +107,32 @@ class Oracle:
         im = OrcImage(blocks.ctypes.data, None if lab is None else lab.ctypes.data, nx, ny, nz,
                       int(dims[0]), int(dims[1]), int(dims[2]), n_phases)
         return im, (blocks, labels)
+
+    def synth_spheres(self, shape, rmin, rmax, porosity, n_phases=1, seed=1):
+        """The benchmark's sphere-pack labels [nz][ny][nx] (0 = pore); returns (labels, porosity)."""
+        nz, ny, nx = shape
+        lab = np.zeros((nz, ny, nx), np.uint8)
+        por = ctypes.c_double(0.0)
+        self.lib.orc_synth_spheres.restype = ctypes.c_int64
+        n = self.lib.orc_synth_spheres(_ptr(lab), nx, ny, nz, ctypes.c_double(rmin), ctypes.c_double(rmax),
+                                       ctypes.c_double(porosity), int(n_phases), ctypes.c_uint64(seed),
+                                       ctypes.byref(por))
+        if n < 0:
+            raise ValueError("orc_synth_spheres rejected its arguments")
+        return lab, por.value
+
+    def place_walkers(self, labels, n, seed, shift=0):
+        """The reference's random placement: (x0, y0, z0, seed0, clamped)."""
+        labels = np.ascontiguousarray(labels, dtype=np.uint8)
+        nz, ny, nx = labels.shape
+        x, y, z = (np.zeros(n, np.int32) for _ in range(3))
+        s = np.zeros(n, np.uint64)
+        clamped = ctypes.c_int64(0)
+        rc = self.lib.orc_place_walkers_random(_ptr(labels), nx, ny, nz, ctypes.c_uint64(seed), ctypes.c_int64(n),
+                                               int(shift), _ptr(x), _ptr(y), _ptr(z), _ptr(s), ctypes.byref(clamped))
+        if rc != 0:
+            raise ValueError("orc_place_walkers_random failed (%d)" % rc)
+        return x, y, z, s, clamped.value
 
     def energy_table(self, f: float, n_max: int):
         t = np.zeros(n_max + 1)
@@ -171,6 +215,26 @@ class Oracle:
             raise ValueError("orc_pfgse rejected its arguments")
         return out
 
+    def pfgse_grad_g(self, labels, walkers, dfactor, steps, kvec, res, kscale, direction, bc="noflux", shift=0,
+                     threads=1, n_phases=None):
+        """FP64 pathwise dM/dg [n_delta][n_g] for k_j = kscale * g_j * direction (unit vector)."""
+        im, keep = self.image(labels, n_phases)
+        x0, y0, z0, s0 = [np.ascontiguousarray(a) for a in walkers]
+        n = len(x0)
+        P = im.n_phases
+        df = np.ascontiguousarray(np.broadcast_to(np.asarray(dfactor, np.float64), (P,)))
+        steps = np.ascontiguousarray(steps, np.int32)
+        kvec = np.ascontiguousarray(kvec, np.float64).reshape(-1, 3)
+        d = np.ascontiguousarray(direction, np.float64)
+        nd, ng = len(steps), len(kvec)
+        out = np.zeros((nd, ng))
+        rc = self.lib.orc_pfgse_grad_g(ctypes.byref(im), BC[bc], shift, ctypes.c_int64(n), _ptr(x0), _ptr(y0),
+                                       _ptr(z0), _ptr(s0), _ptr(df), nd, _ptr(steps), ng, _ptr(kvec),
+                                       ctypes.c_double(res), ctypes.c_double(kscale), _ptr(d), _ptr(out), threads)
+        if rc != 0:
+            raise ValueError("orc_pfgse_grad_g rejected its arguments")
+        return out
+
     def displacements(self, labels, walkers, steps, bc="noflux", shift=0, threads=1, n_phases=None):
         im, keep = self.image(labels, n_phases)
         x0, y0, z0, s0 = [np.ascontiguousarray(a) for a in walkers]
@@ -201,7 +265,7 @@ class RefSimParams(ctypes.Structure):
         ("n_rho", ctypes.c_int32), ("d0", ctypes.c_double), ("bulk_time", ctypes.c_double),
         ("steps_per_echo", ctypes.c_int32), ("bc", ctypes.c_char_p), ("resolution", ctypes.c_double),
         ("voxel_division", ctypes.c_int32), ("gamma", ctypes.c_double), ("gamma_unit", ctypes.c_char_p),
-        ("histograms", ctypes.c_int32), ("histogram_size", ctypes.c_int32),
+        ("histograms", ctypes.c_int32), ("histogram_size", ctypes.c_int32), ("histogram_scale", ctypes.c_char_p),
     ]
 
 
@@ -229,14 +293,16 @@ class RefSim:
 
     def __init__(self, labels, walkers, seed, rho=(0.0,), d0=2.5, bulk_time=2800.0, steps_per_echo=1,
                  bc="noflux", resolution=1.0, voxel_division=0, placement="random", deviation=0,
-                 rho_type="uniform", gamma=42.576, gamma_unit="mhertz"):
+                 rho_type="uniform", gamma=42.576, gamma_unit="mhertz", histograms=1, histogram_size=1024,
+                 histogram_scale="linear"):
         L = self.lib()
         self.labels = np.ascontiguousarray(labels, dtype=np.uint8)
         nz, ny, nx = self.labels.shape
         self._rho = (ctypes.c_double * len(rho))(*rho)
         p = RefSimParams(int(walkers), int(seed), placement.encode(), int(deviation), rho_type.encode(), self._rho,
                          len(rho), float(d0), float(bulk_time), int(steps_per_echo), bc.encode(), float(resolution),
-                         int(voxel_division), float(gamma), gamma_unit.encode(), 1, 1024)
+                         int(voxel_division), float(gamma), gamma_unit.encode(), int(histograms), int(histogram_size),
+                         histogram_scale.encode())
         self.workdir = tempfile.mkdtemp(prefix="rwnmr_ref_")
         self.h = L.ref_sim_create(self.workdir.encode(), _ptr(self.labels), nx, ny, nz, ctypes.byref(p))
         info = np.zeros(12, np.int64)
@@ -290,6 +356,25 @@ class RefSim:
         if n < 0:
             raise ValueError("cap too small")
         return dict(raw=raw[:n].copy(), signal=out[:n].copy(), times=times[:n].copy(), map_collisions=mc)
+
+    def cpmg_method(self, method, obs_time, apply_bulk=True, cap=1 << 20, hcap=1 << 14):
+        """NMR_cpmg::set + run_simulation with METHOD ``method`` ("image-based" | "histogram"):
+        the decay (raw and normalised) and the xi-rate histograms of the collision-mapping walk."""
+        L = self.lib()
+        L.ref_cpmg_method.restype = ctypes.c_int
+        raw, out, times = np.zeros(cap), np.zeros(cap), np.zeros(cap)
+        hb, ha = np.zeros(hcap), np.zeros(hcap)
+        nmax = 64
+        lb, la = np.zeros(nmax * hcap), np.zeros(nmax * hcap)
+        sizes = np.zeros(2, np.int32)
+        n = L.ref_cpmg_method(_vp(self.h), method.encode(), ctypes.c_double(obs_time), int(apply_bulk), _ptr(raw),
+                              _ptr(out), _ptr(times), cap, _ptr(hb), _ptr(ha), _ptr(lb), _ptr(la), hcap, _ptr(sizes))
+        hs, nl = int(sizes[0]), int(sizes[1])
+        if n < 0 or nl > nmax:
+            raise ValueError("cap too small")
+        return dict(raw=raw[:n].copy(), signal=out[:n].copy(), times=times[:n].copy(), hist_bins=hb[:hs].copy(),
+                    hist_amps=ha[:hs].copy(), list_bins=lb[: nl * hs].reshape(nl, hs).copy(),
+                    list_amps=la[: nl * hs].reshape(nl, hs).copy())
 
     def multitau(self, cpmg_text, multitau_text, cap=256):
         """The reference's NMR_multitau::run on CPU; returns steps per echo, echo times, first echoes."""

@@ -73,6 +73,7 @@ struct ref_sim_params
     const char *gamma_unit; // "mhertz" | "rad"
     int32_t histograms;
     int32_t histogram_size;
+    const char *histogram_scale; // "linear" | "log"
 };
 
 struct ref_handle
@@ -133,7 +134,7 @@ std::string rwnmr_text(const ref_sim_params &p)
     o << "SAVE_IMG_INFO: false\nSAVE_BINIMG: false\nSAVE_WALKERS: false\n";
     o << "HISTOGRAMS: " << p.histograms << "\n";
     o << "HISTOGRAM_SIZE: " << p.histogram_size << "\n";
-    o << "HISTOGRAM_SCALE: linear\n";
+    o << "HISTOGRAM_SCALE: " << p.histogram_scale << "\n";
     o << "OPENMP_USAGE: false\nOPENMP_THREADS: 1\n";
     o << "GPU_USAGE: false\nBLOCKS: 4096\nTHREADSPERBLOCK: 1024\nECHOESPERKERNEL: 16\n";
     o << "REDUCE_IN_GPU: true\nMAX_RWSTEPS: 65536\n";
@@ -374,6 +375,64 @@ int ref_cpmg(void *hv, double obs_time, int apply_bulk, double *raw, double *out
     cpmg.normalizeSignal();
     for (int i = 0; i < n; i++) out[i] = cpmg.signal_amps[i];
     for (int i = 0; i < n && i < (int)cpmg.signal_times.size(); i++) times[i] = cpmg.signal_times[i];
+    return n;
+}
+
+// The reference's CPMG sequence with a chosen METHOD ("image-based" or "histogram"): NMR_cpmg::set()
+// (collision-mapping walk with HISTOGRAMS windows, xi-rate histograms, relaxivity update;
+// NMR_cpmg.cpp:112-146, NMR_Simulation.cpp:1456-1479, 1787-1841) and the body of
+// NMR_cpmg::run_simulation (NMR_cpmg.cpp:149-175): the image-based walk, or createPenaltiesVector +
+// histogram_simulation (NMR_cpmg.cpp:235-343); then applyBulk and normalizeSignal.
+//   raw[], out[], times[]: as ref_cpmg. hist_bins/hist_amps [histogram size]: the global xi-rate
+//   histogram (NMR_Simulation::histogram); list_bins/list_amps [n_list][histogram size]: the
+//   per-window histograms (NMR_Simulation::histogramList). sizes[0] <- histogram size,
+//   sizes[1] <- number of windows. Returns the number of echo values, or -1 if a cap is too small.
+int ref_cpmg_method(void *hv, const char *method, double obs_time, int apply_bulk, double *raw, double *out,
+                    double *times, int cap, double *hist_bins, double *hist_amps, double *list_bins, double *list_amps,
+                    int hcap, int32_t *sizes)
+{
+    ref_handle *h = (ref_handle *)hv;
+    NMR_Simulation &s = *h->sim;
+    std::ostringstream c;
+    c << "METHOD: " << method << "\nOBS_TIME: " << fmt_double(obs_time)
+      << "\nAPPLY_BULK: " << (apply_bulk ? "true" : "false")
+      << "\nTIME_VERBOSE: false\nRESIDUAL_FIELD: none\nSAVE_MODE: false\n";
+    write_file(h->workdir + "/config/default/cpmg.config", c.str());
+    cwd_guard g(h->workdir);
+    cpmg_config cfg(std::string(CONFIG_ROOT) + CPMG_CONFIG_DEFAULT);
+    NMR_cpmg cpmg(s, cfg);
+    cpmg.set();
+    if (cpmg.getMethod() == "histogram")
+    {
+        std::vector<double> rho = s.rwNMR_config.getRho();
+        if (s.rwNMR_config.getRhoType() == "uniform") cpmg.createPenaltiesVector(rho[0]);
+        else cpmg.createPenaltiesVector(rho);
+        cpmg.histogram_simulation();
+    }
+    else
+        cpmg.image_simulation_omp();
+    const int n = (int)cpmg.signal_amps.size();
+    const int hs = s.histogram.getSize();
+    const int nl = (int)s.histogramList.size();
+    sizes[0] = hs;
+    sizes[1] = nl;
+    if (n > cap || hs > hcap || (int)s.histogram.bins.size() != hs) return -1;
+    for (int i = 0; i < n; i++) raw[i] = cpmg.signal_amps[i];
+    if (cpmg.getApplyBulkRelaxation()) cpmg.applyBulk();
+    cpmg.normalizeSignal();
+    for (int i = 0; i < n; i++) out[i] = cpmg.signal_amps[i];
+    for (int i = 0; i < n && i < (int)cpmg.signal_times.size(); i++) times[i] = cpmg.signal_times[i];
+    for (int i = 0; i < hs; i++)
+    {
+        hist_bins[i] = s.histogram.bins[i];
+        hist_amps[i] = s.histogram.amps[i];
+    }
+    for (int l = 0; l < nl && list_bins; l++)
+        for (int i = 0; i < hs; i++)
+        {
+            list_bins[(size_t)l * hs + i] = s.histogramList[l].bins[i];
+            list_amps[(size_t)l * hs + i] = s.histogramList[l].amps[i];
+        }
     return n;
 }
 

@@ -5,8 +5,10 @@
 
 #include "rwnmr_oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <random>
 #include <vector>
 #include <omp.h>
 
@@ -512,6 +514,68 @@ int orc_pfgse(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const 
     return 0;
 }
 
+// Pathwise FP64 derivative of the PFGSE phase sums with respect to the gradient strength g, for a
+// gradient ramp k_j = kscale * g_j * dir (kscale = dk/dg, NMR_pfgse.cpp:483-486; dir a unit
+// vector). For fixed trajectories M_j = sum_w E_w cos((k_j . dR_w) res), so
+//   dM_j/dg = -sum_w E_w sin((k_j . dR_w) res) * (kscale dir . dR_w) res,
+// evaluated per walker in FP64 (the same walks, energies and k . dR as orc_pfgse) and summed in
+// the walker order of each thread's contiguous range, then over threads in order.
+int orc_pfgse_grad_g(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const int32_t *x0,
+                     const int32_t *y0, const int32_t *z0, const uint64_t *seed0, const double *dfactor,
+                     int32_t n_delta, const int32_t *steps, int32_t n_g, const double *kvec, double res, double kscale,
+                     const double *dir, double *dMdg, int32_t threads)
+{
+    if (!image_ok(img) || n < 0 || n_delta < 0 || n_g < 0 || shift < 0 || !dfactor || !dir || !dMdg ||
+        (n_delta > 0 && !steps))
+        return -1;
+    for (int32_t i = 1; i < n_delta; i++)
+        if (steps[i] < steps[i - 1]) return -1;
+    const int P = img->n_phases;
+    Tables tab;
+    tab.build(dfactor, P, n_delta ? steps[n_delta - 1] : 0);
+    const int nt = threads > 1 ? threads : 1;
+    std::vector<double> acc((size_t)nt * n_delta * n_g, 0.0);
+#pragma omp parallel num_threads(nt)
+    {
+        int t = omp_get_thread_num();
+        int64_t lo = n * t / nt, hi = n * (t + 1) / nt;
+        double *a = &acc[(size_t)t * n_delta * n_g];
+        std::vector<uint32_t> c(P);
+        for (int64_t i = lo; i < hi; i++)
+        {
+            Walk w{x0[i], y0[i], z0[i], seed0[i]};
+            std::fill(c.begin(), c.end(), 0u);
+            int32_t done = 0;
+            for (int32_t d = 0; d < n_delta; d++)
+            {
+                for (; done < steps[d]; done++)
+                {
+                    int ph = step(*img, bc, shift, w);
+                    if (ph >= 0) c[ph]++;
+                }
+                const double e = tab.energy(c.data());
+                const double dX = (double)w.x - (double)x0[i];
+                const double dY = (double)w.y - (double)y0[i];
+                const double dZ = (double)w.z - (double)z0[i];
+                const double proj = kscale * (dir[0] * dX + dir[1] * dY + dir[2] * dZ) * res;
+                for (int32_t j = 0; j < n_g; j++)
+                {
+                    const double kd = kvec[3 * j + 0] * dX + kvec[3 * j + 1] * dY + kvec[3 * j + 2] * dZ;
+                    a[(size_t)d * n_g + j] -= e * std::sin(kd * res) * proj;
+                }
+            }
+        }
+    }
+    for (int32_t d = 0; d < n_delta; d++)
+        for (int32_t j = 0; j < n_g; j++)
+        {
+            double s = 0.0;
+            for (int t = 0; t < nt; t++) s += acc[((size_t)t * n_delta + d) * n_g + j];
+            dMdg[(size_t)d * n_g + j] = s;
+        }
+    return 0;
+}
+
 int orc_displacements(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const int32_t *x0,
                       const int32_t *y0, const int32_t *z0, const uint64_t *seed0, int32_t steps, int32_t *dx,
                       int32_t *dy, int32_t *dz, uint32_t *collf, int32_t threads)
@@ -540,6 +604,119 @@ int orc_displacements(const orc_image *img, int32_t bc, int32_t shift, int64_t n
         if (collf)
             for (int q = 0; q < P; q++) collf[(size_t)i * P + q] = c[q];
     }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Synthetic inputs for the CPU reference arm of the benchmark, so that it needs no product code.
+
+// The benchmark's overlapping-sphere packs: centre uniform in the box, radius uniform in
+// [rmin, rmax], label uniform in 1..n_phases, spheres added until at most floor(porosity * volume)
+// voxels are pore. Draws are splitmix64 outputs (Steele, Lea & Flood 2014) turned into doubles in
+// [0, 1) from their top 53 bits, four per sphere in the order cx, cy, cz, r, label; a voxel is in a
+// sphere when its squared distance from the centre is at most r^2 (later spheres relabel).
+int64_t orc_synth_spheres(uint8_t *labels, int32_t nx, int32_t ny, int32_t nz, double rmin, double rmax,
+                          double porosity, int32_t n_phases, uint64_t seed, double *porosity_out)
+{
+    if (!labels || nx <= 0 || ny <= 0 || nz <= 0 || rmin < 0 || rmax < rmin || n_phases < 1 || n_phases > 255)
+        return -1;
+    uint64_t state = seed;
+    auto draw = [&state]() {
+        uint64_t v = (state += 0x9E3779B97F4A7C15ull);
+        v = (v ^ (v >> 30)) * 0xBF58476D1CE4E5B9ull;
+        v = (v ^ (v >> 27)) * 0x94D049BB133111EBull;
+        v ^= v >> 31;
+        return (double)(v >> 11) / 9007199254740992.0;
+    };
+    const int64_t volume = (int64_t)nx * ny * nz;
+    std::fill(labels, labels + volume, (uint8_t)0);
+    int64_t pore = volume, spheres = 0;
+    const int64_t goal = (int64_t)std::floor(porosity * (double)volume);
+    while (pore > goal)
+    {
+        const double cx = draw() * nx, cy = draw() * ny, cz = draw() * nz;
+        const double r = rmin + (rmax - rmin) * draw();
+        int lab = 1 + (int)(draw() * n_phases);
+        if (lab > n_phases) lab = n_phases;
+        for (int z = std::max(0, (int)std::ceil(cz - r)); z <= std::min(nz - 1, (int)std::floor(cz + r)); z++)
+            for (int y = std::max(0, (int)std::ceil(cy - r)); y <= std::min(ny - 1, (int)std::floor(cy + r)); y++)
+            {
+                const double d2 = (z - cz) * (z - cz) + (y - cy) * (y - cy);
+                if (d2 > r * r) continue;
+                for (int x = std::max(0, (int)std::ceil(cx - r)); x <= std::min(nx - 1, (int)std::floor(cx + r)); x++)
+                {
+                    if (d2 + (x - cx) * (x - cx) > r * r) continue;
+                    uint8_t &v = labels[((int64_t)z * ny + y) * nx + x];
+                    pore -= v == 0;
+                    v = (uint8_t)lab;
+                }
+            }
+        spheres++;
+    }
+    if (porosity_out) *porosity_out = (double)pore / (double)volume;
+    return spheres;
+}
+
+// The reference's uniformly random walker placement with its seeds, draw for draw
+// (NMR_Simulation/NMR_Simulation.cpp): std::mt19937 seeded with SEED then discard(4096)
+// (:86-95); one uniform_int_distribution<uint64_t> seed per walker (createWalkers, :1139-1204);
+// pore voxels listed in z, y, x order (createPoreList, :930-980); the pore count re-derived as
+// (uint)(porosity * volume) and n pore ids drawn from uniform_int_distribution(0, that count), which
+// includes one past the end (updateNumberOfPores, createWalkersIDList, :904-907, 1086-1136) -- an id
+// past the list is clamped to its last pore and counted in *clamped; with every pore occupied the
+// walkers take the pores in order (placeWalkersUniformly, :1271-1333); voxel division then draws x,
+// y, z offsets per walker (applyVoxelDivision, :192-268). labels: [nz][ny][nx], non-zero = solid.
+int orc_place_walkers_random(const uint8_t *labels, int32_t nx, int32_t ny, int32_t nz, uint64_t seed, int64_t n,
+                             int32_t shift, int32_t *x0, int32_t *y0, int32_t *z0, uint64_t *seed0, int64_t *clamped)
+{
+    if (!labels || nx <= 0 || ny <= 0 || nz <= 0 || seed == 0 || n < 0 || n > 0xffffffffll || shift < 0 || shift > 10)
+        return -1;
+    std::mt19937 mt((std::mt19937::result_type)seed);
+    mt.discard(4096);
+    std::vector<int32_t> px, py, pz;
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++)
+                if (!labels[((int64_t)z * ny + y) * nx + x])
+                {
+                    px.push_back(x);
+                    py.push_back(y);
+                    pz.push_back(z);
+                }
+    if (px.empty()) return -2;
+    const double volume = (double)nx * ny * nz;
+    const double occupancy = (double)n / (double)px.size();
+    std::uniform_int_distribution<uint64_t> seeds;
+    for (int64_t i = 0; i < n; i++) seed0[i] = seeds(mt);
+    std::uniform_int_distribution<std::mt19937::result_type> pick(
+        0, (std::mt19937::result_type)((double)px.size() / volume * volume));
+    std::vector<uint64_t> ids((size_t)n);
+    for (int64_t i = 0; i < n; i++) ids[i] = pick(mt);
+    int64_t clamp = 0;
+    for (int64_t i = 0; i < n; i++)
+    {
+        uint64_t id = occupancy != 1.0 ? ids[i] : (uint64_t)i;
+        if (id >= px.size())
+        {
+            id = px.size() - 1;
+            clamp++;
+        }
+        x0[i] = px[id];
+        y0[i] = py[id];
+        z0[i] = pz[id];
+    }
+    if (shift > 0)
+    {
+        const std::mt19937::result_type factor = 1u << shift;
+        std::uniform_int_distribution<std::mt19937::result_type> sub(0, factor - 1);
+        for (int64_t i = 0; i < n; i++)
+        {
+            x0[i] = (int32_t)((double)x0[i] * factor + (double)sub(mt));
+            y0[i] = (int32_t)((double)y0[i] * factor + (double)sub(mt));
+            z0[i] = (int32_t)((double)z0[i] * factor + (double)sub(mt));
+        }
+    }
+    if (clamped) *clamped = clamp;
     return 0;
 }
 

@@ -67,6 +67,12 @@ int orc_pfgse(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const 
               int32_t n_g, const double *kvec, double res, double *M, double *esum, uint64_t *msd, uint64_t *esum_fx,
               int32_t threads);
 
+// dM/dg of the PFGSE phase sums along a gradient ramp k_j = kscale g_j dir (FP64, pathwise).
+int orc_pfgse_grad_g(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const int32_t *x0,
+                     const int32_t *y0, const int32_t *z0, const uint64_t *seed0, const double *dfactor,
+                     int32_t n_delta, const int32_t *steps, int32_t n_g, const double *kvec, double res, double kscale,
+                     const double *dir, double *dMdg, int32_t threads);
+
 /* The reference's uniform internal field (NMR_Simulation/InternalField.cpp, fillDataArray):
  * out[(z*ny + y)*nx + x] = coord * dG in pore voxels and 0 in solid ones, coord the voxel's
  * x, y or z (direction 0/1/2) and dG = gradient * 1e-6 * resolution. */
@@ -96,6 +102,16 @@ int orc_cpmg_field(const orc_image *img, int32_t bc, int32_t shift, int64_t n, c
 int orc_displacements(const orc_image *img, int32_t bc, int32_t shift, int64_t n, const int32_t *x0,
                       const int32_t *y0, const int32_t *z0, const uint64_t *seed0, int32_t steps, int32_t *dx,
                       int32_t *dy, int32_t *dz, uint32_t *collf, int32_t threads);
+
+// Synthetic sphere-pack labels [nz][ny][nx] (0 = pore) for the CPU reference arm; returns the
+// sphere count, or -1 on bad arguments.
+int64_t orc_synth_spheres(uint8_t *labels, int32_t nx, int32_t ny, int32_t nz, double rmin, double rmax,
+                          double porosity, int32_t n_phases, uint64_t seed, double *porosity_out);
+
+// The reference's random walker placement (seeds, then pore ids, then sub-voxel offsets).
+// Returns 0, -1 on bad arguments, -2 for an image without pores.
+int orc_place_walkers_random(const uint8_t *labels, int32_t nx, int32_t ny, int32_t nz, uint64_t seed, int64_t n,
+                             int32_t shift, int32_t *x0, int32_t *y0, int32_t *z0, uint64_t *seed0, int64_t *clamped);
 
 #ifdef __cplusplus
 }

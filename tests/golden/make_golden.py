@@ -4,13 +4,17 @@ The reference (RandomWalk_NMR) ships no tests or golden vectors, so the fixtures
 running its unmodified CPU sources, compiled by oracle/Makefile into oracle/_ref/librwnmr_ref.so,
 through oracle/ref_driver.cpp. Run from the repository root where the reference sources exist:
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    RWNMR_REFERENCE=<RandomWalk_NMR checkout> python tests/golden/make_golden.py
+
+(the checkout defaults to /root/reference, where this script was written against a read-only copy);
+the script builds oracle/_ref from that checkout first.
 
 Images come from the repository's sphere-pack generator (randomwalk_nmr_gb300.host), so the
 fixtures pin the reference's setup, walk, CPMG and PFGSE outputs on fixed inputs.
 """
 from __future__ import annotations
 
+import hashlib
 import os
 import sys
 
@@ -20,6 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
+from oracle import pyoracle  # noqa: E402
 from oracle.pyoracle import RefSim, ref_bitblock  # noqa: E402
 from randomwalk_nmr_gb300 import host  # noqa: E402
 
@@ -35,6 +40,7 @@ def image_a():
 
 
 def main():
+    pyoracle.build(with_ref=True, ref_root=os.environ.get(pyoracle.REF_ENV, "/root/reference"))
     out = {}
     lab = image_a()
     out["img_a"] = lab
@@ -101,6 +107,25 @@ def main():
     out.update(multitau_steps=mt["steps"], multitau_times=mt["times"], multitau_amps=mt["amps"])
     del rs6
 
+    # METHOD: histogram (createPenaltiesVector + histogram_simulation, NMR_cpmg.cpp:235-343) and the
+    # xi-rate collision histograms of the mapping walk (CollisionHistogram.cpp:59-249), for uniform
+    # and sigmoid relaxivity, linear and log bins, several histogram windows; plus the image-based
+    # method on the same setup, whose histograms come from the same mapping walk.
+    hm_cases = [("hm_u", (25.0,), "uniform", 4, 256, "linear", "histogram"),
+                ("hm_s", sig, "sigmoid", 3, 128, "linear", "histogram"),
+                ("hm_l", (25.0,), "uniform", 2, 64, "log", "histogram"),
+                ("hm_i", (25.0,), "uniform", 4, 256, "linear", "image-based")]
+    for key, rho, rtype, nh, hs, scale, method in hm_cases:
+        r = RefSim(lab, 400, 5, rho=rho, rho_type=rtype, steps_per_echo=3, bulk_time=800.0, histograms=nh,
+                   histogram_size=hs, histogram_scale=scale)
+        c = r.cpmg_method(method, obs_time=12.0, apply_bulk=True)
+        out[f"{key}_args"] = np.array([nh, hs], np.int64)
+        out[f"{key}_scale"] = np.array(scale)
+        out[f"{key}_method"] = np.array(method)
+        out[f"{key}_rho"] = np.array(rho)
+        out.update({f"{key}_{k}": v for k, v in c.items()})
+        del r
+
     # walker placement modes (no one-past-the-end pore draws in these cases)
     lab_p = lab.copy()
     nz, ny, nx = lab_p.shape
@@ -119,6 +144,50 @@ def main():
 
     np.savez_compressed(os.path.join(HERE, "reference_cpu.npz"), **out)
     print("wrote", os.path.join(HERE, "reference_cpu.npz"))
+    full_size()
+
+
+def full_size():
+    """Fixtures at full image sizes of the benchmark configurations.
+
+    * plain CPMG, 100^3 (spheres of radius 4-10 to porosity 0.30, seed 1), 10,000 walkers placed
+      with SEED 7, rho 10 um/s, 2000 echoes x 3 steps: the reference's own walk (Walker::walk /
+      Walker::map in the serial order of NMR_cpmg::image_simulation_omp, NMR_cpmg.cpp:177-233):
+      echo sums, per-echo collisions, final positions, RNG states and collision counts;
+    * PFGSE, 256^3 (radius 5-15, porosity 0.35, seed 3), 64 gradients 0-100 G/cm along z, pulse
+      1 ms, 10 exposure times log-spaced 1-100 ms, rho 10 um/s: the reference's CPU sequence
+      (NMR_PFGSE::run, NMR_pfgse.cpp:98-131, 1658-1806) on 16,384 walkers placed with SEED 7.
+    """
+    out = {}
+    lab, _ = host.synth_spheres((100, 100, 100), 4.0, 10.0, 0.30, 1, seed=1)
+    blocks, dims = ref_bitblock(lab)
+    out.update(c1_blocks=blocks, c1_bdims=dims)
+    rs = RefSim(lab, 10_000, 7, rho=(10.0,), steps_per_echo=3, bulk_time=2800.0)
+    x, y, z, s, df = rs.walkers()
+    out.update(c1_x0=x, c1_y0=y, c1_z0=z, c1_seed0=s, c1_dfactor=df)
+    r1 = rs.walk(1, 2000, 3)
+    r0 = rs.walk(0, 2000, 3)
+    out.update(c1_energy_sum=r1["per_echo"], c1_coll_per_echo=r0["per_echo"], c1_xf=r1["xf"], c1_yf=r1["yf"],
+               c1_zf=r1["zf"], c1_seedf=r1["seed"], c1_coll=r0["coll"], c1_energy=r1["energy"])
+    del rs
+    np.savez_compressed(os.path.join(HERE, "reference_c1.npz"), **out)
+    print("wrote", os.path.join(HERE, "reference_c1.npz"))
+
+    out = {}
+    lab, _ = host.synth_spheres((256, 256, 256), 5.0, 15.0, 0.35, 1, seed=3)
+    blocks, dims = ref_bitblock(lab)
+    out["c3_blocks_sha256"] = np.array(hashlib.sha256(blocks.tobytes()).hexdigest())
+    out["c3_bdims"] = dims
+    rs = RefSim(lab, 16_384, 7, rho=(10.0,), steps_per_echo=1, bulk_time=2800.0)
+    pf = rs.pfgse(pulse_width=1.0, gmax=(0.0, 0.0, 100.0), n_g=64, time_seq="log", n_t=10, t_min=0.0, t_max=2.0,
+                  threshold_type="samples", threshold_value=64)
+    x, y, z, s, df = rs.walkers()
+    out.update(c3_x0=x, c3_y0=y, c3_z0=z, c3_seed0=s, c3_dfactor=df, c3_Mkt=pf["Mkt"], c3_steps=pf["steps"],
+               c3_dsat=pf["dsat"], c3_dmsd=pf["dmsd"], c3_kvec=pf["kvec"], c3_delta=pf["delta"],
+               c3_gamma=np.array(rs.info["gamma"]), c3_dt=np.array(rs.info["dt"]))
+    del rs
+    np.savez_compressed(os.path.join(HERE, "reference_c3.npz"), **out)
+    print("wrote", os.path.join(HERE, "reference_c3.npz"))
 
 
 if __name__ == "__main__":

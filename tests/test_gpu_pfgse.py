@@ -108,6 +108,26 @@ def test_pfgse_grad_g_matches_finite_differences(engine, gdir):
     np.testing.assert_allclose(dM, fd, rtol=1e-5, atol=1e-7 * len(w[0]))
 
 
+@pytest.mark.parametrize("gdir", [(0, 0, 1.0), (1.0, 0, 0), (0.6, 0.0, 0.8), (1.0, 1.0, 1.0)])
+@pytest.mark.parametrize("bc", ["noflux", "periodic"])
+def test_pfgse_grad_g_matches_fp64_pathwise_oracle(engine, oracle, gdir, bc):
+    """rwnmr_pfgse_grad_g against the oracle's FP64 pathwise dM/dg on the same trajectories:
+    relative 1e-10 (the GPU's energies are rounded once to 2^-63, its sines to 2^-61), with an
+    absolute floor of 1e-12 of the largest derivative for entries that cancel to near zero."""
+    lab, w = setup(engine, seed=5)
+    steps = np.array([30, 120, 400], np.int32)
+    d = np.asarray(gdir, np.float64)
+    d = d / np.linalg.norm(d)
+    kscale = (1.0 * 1e-3) * (42.576 * 2 * np.pi * 1e6) * 1e-8
+    gvals = np.linspace(0.0, 120.0, 9)
+    kv = np.outer(gvals * kscale, d)
+    f = dfactor(10.0)
+    dM = engine.pfgse_grad_g(steps, kv, 1.0, f, kscale, d, bc=bc)
+    o = oracle.pfgse_grad_g(lab, w, f, steps, kv, 1.0, kscale, d, bc=bc, threads=4)
+    assert np.all(dM[:, 0] == 0.0)
+    np.testing.assert_allclose(dM, o, rtol=1e-10, atol=1e-12 * np.abs(o).max())
+
+
 def test_pfgse_per_walker_dfactor(engine, golden):
     """RHO_TYPE sigmoid: the reference's per-walker decrease factors give its attenuations; equal
     per-walker factors reproduce the per-phase tables on both the axis and the general path."""

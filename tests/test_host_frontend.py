@@ -11,7 +11,8 @@ import pytest
 
 from randomwalk_nmr_gb300.engine import load_library
 
-REF_IMAGES = "/root/reference/input/images/tiny_3D"
+# the reference's sample PNG stack, from a RandomWalk_NMR checkout named by $RWNMR_REFERENCE
+REF_IMAGES = os.path.join(os.environ.get("RWNMR_REFERENCE", ""), "input", "images", "tiny_3D")
 
 
 def config_json(kind, root, user="default"):
@@ -188,7 +189,8 @@ def test_png_decoder_matches_encoder(tmp_path, color_type, bit_depth):
     assert np.array_equal(mask.astype(bool), solid)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_IMAGES), reason="reference sample images not present")
+@pytest.mark.skipif(not os.environ.get("RWNMR_REFERENCE") or not os.path.isdir(REF_IMAGES),
+                    reason="reference sample images not present (set RWNMR_REFERENCE)")
 def test_reference_sample_slices_decode():
     from randomwalk_nmr_gb300.host import png_mask
 

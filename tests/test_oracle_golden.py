@@ -106,3 +106,86 @@ def test_energy_table_fixed_point(oracle):
         acc = acc * 0.99
         assert t[k] == acc
         assert int(fx[k]) == round(acc * 2.0**63)
+
+
+# -- full image sizes of the benchmark configurations (tests/golden/reference_c1.npz, reference_c3.npz)
+import os  # noqa: E402
+
+import pytest  # noqa: E402
+
+from conftest import ROOT  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return dict(np.load(os.path.join(ROOT, "tests", "golden", "reference_c1.npz")))
+
+
+@pytest.fixture(scope="module")
+def c3():
+    return dict(np.load(os.path.join(ROOT, "tests", "golden", "reference_c3.npz")))
+
+
+def test_c1_full_size_walk_matches_reference(c1, oracle):
+    """100^3 sphere pack, 10,000 walkers, 2000 echoes x 3 steps (6e7 walker-steps): the host's
+    image and placement and the restated walk against the reference's own CPU walk."""
+    lab, _ = host.synth_spheres((100, 100, 100), 4.0, 10.0, 0.30, 1, seed=1)
+    blocks, dims = host.pack_blocks(lab)
+    assert np.array_equal(blocks, c1["c1_blocks"]) and list(dims) == list(c1["c1_bdims"])
+    x, y, z, s, info = host.place_walkers(blocks, lab.shape, 10_000, 7)
+    for a, k in ((x, "x0"), (y, "y0"), (z, "z0"), (s, "seed0")):
+        assert np.array_equal(a, c1["c1_" + k])
+    f = float(c1["c1_dfactor"][0])
+    out = oracle.cpmg(lab, (x, y, z, s), 2000, 3, f, threads=1)
+    # one thread: the reference's serial walker order, so even the FP64 echo sums are bit-exact
+    assert np.array_equal(out["echo_fp64"], c1["c1_energy_sum"])
+    assert np.array_equal(out["echo_coll"][:, 0], c1["c1_coll_per_echo"])
+    for a, k in (("xf", "xf"), ("yf", "yf"), ("zf", "zf"), ("seedf", "seedf")):
+        assert np.array_equal(out[a], c1["c1_" + k])
+    assert np.array_equal(out["collf"][:, 0], c1["c1_coll"])
+
+
+def test_c3_full_size_pfgse_matches_reference(c3, oracle):
+    """256^3 sphere pack, 64 gradients 0-100 G/cm along z, 10 exposure times 1-100 ms log-spaced
+    (cumulative walk to 1500 steps), 16,384 walkers: the restated PFGSE sums against the reference's
+    own CPU sequence: bit-exact in the reference's serial walker order."""
+    import hashlib
+
+    lab, _ = host.synth_spheres((256, 256, 256), 5.0, 15.0, 0.35, 1, seed=3)
+    blocks, dims = host.pack_blocks(lab)
+    assert hashlib.sha256(blocks.tobytes()).hexdigest() == str(c3["c3_blocks_sha256"])
+    x, y, z, s, info = host.place_walkers(blocks, lab.shape, 16_384, 7)
+    for a, k in ((x, "x0"), (y, "y0"), (z, "z0"), (s, "seed0")):
+        assert np.array_equal(a, c3["c3_" + k])
+    f = float(c3["c3_dfactor"][0])
+    out = oracle.pfgse(lab, (x, y, z, s), f, c3["c3_steps"], c3["c3_kvec"], 1.0, threads=1)
+    Mkt = out["M"] / out["esum"][:, None]
+    assert np.array_equal(Mkt, c3["c3_Mkt"])
+
+
+def test_oracle_inputs_match_reference_placement_and_library_generator(golden, c1, c3, oracle):
+    """The oracle's own sphere packs and random placement (used by the benchmark's CPU reference
+    arm, which loads no product code): the library's generator gives the same bytes, and the
+    placement is the reference's, draw for draw (golden placement fixtures and the full-size sets)."""
+    for args in (((20, 18, 22), 2.0, 5.0, 0.4, 4, 23), ((100, 100, 100), 4.0, 10.0, 0.30, 1, 1),
+                 ((33, 17, 41), 1.0, 3.5, 0.2, 2, 9)):
+        a, pa = oracle.synth_spheres(*args)
+        b, pb = host.synth_spheres(*args[:5], seed=args[5])
+        assert np.array_equal(a, b) and pa == pb
+    lab = golden["img_p"]
+    k = 0
+    while f"place{k}_args" in golden:
+        dev, shift, n, seed = (int(v) for v in golden[f"place{k}_args"])
+        if str(golden[f"place{k}_mode"]) == "random":
+            x, y, z, s, clamped = oracle.place_walkers(lab, n, seed, shift)
+            assert clamped == 0
+            for a, key in ((x, "x"), (y, "y"), (z, "z"), (s, "seed")):
+                assert np.array_equal(a, golden[f"place{k}_{key}"]), (k, key)
+        k += 1
+    lab1, _ = oracle.synth_spheres((100, 100, 100), 4.0, 10.0, 0.30, 1, 1)
+    assert np.array_equal(oracle.pack_blocks(lab1)[0], c1["c1_blocks"])
+    x, y, z, s, _ = oracle.place_walkers(lab1, 10_000, 7)
+    assert np.array_equal(x, c1["c1_x0"]) and np.array_equal(z, c1["c1_z0"]) and np.array_equal(s, c1["c1_seed0"])
+    lab3, _ = oracle.synth_spheres((256, 256, 256), 5.0, 15.0, 0.35, 1, 3)
+    x, y, z, s, _ = oracle.place_walkers(lab3, 16_384, 7)
+    assert np.array_equal(y, c3["c3_y0"]) and np.array_equal(s, c3["c3_seed0"])
