@@ -8,6 +8,10 @@
 // takes device pointers for every input and output and keeps its own scratch -- the energy tables,
 // the per-echo fixed-point accumulators and a status word -- in the file-scope device array below.
 //
+// The energy tables are filled on the GPU by one thread per phase, as the FP64 repeated product the
+// reference computes one collision at a time, so they are bit-identical to the context path's host
+// tables; that serial chain adds latency in proportion to the table length (echoes x steps per echo).
+//
 // Limits and sharing:
 //   * the scratch array is kNoallocScratchBytes (8 MiB) on every device that loads the library,
 //     held until the process exits; a request whose tables plus accumulators do not fit is
@@ -60,6 +64,25 @@ __global__ void noalloc_tables_kernel(unsigned long long *tab, int slots, int n_
     }
 }
 
+// The exact 128-bit integer l0 + l1 2^21 + l2 2^42 (three u64 limb sums) rounded once to FP64
+// (round to nearest, ties to even) and scaled by 2^-63: the same value the context entry point's
+// host-side conversion gives. The top 64 significant bits, with a sticky bit for any nonzero bits
+// below them, convert with one rounding; the power-of-two scalings are exact.
+__device__ double limbs_to_double_rn(const unsigned long long *a)
+{
+    unsigned long long lo = a[0], hi = 0;
+    const unsigned long long t1 = a[1] << 21, t2 = a[2] << 42;
+    lo += t1;
+    hi += (a[1] >> 43) + (lo < t1 ? 1ull : 0ull);
+    lo += t2;
+    hi += (a[2] >> 22) + (lo < t2 ? 1ull : 0ull);
+    if (hi == 0) return ldexp(__ull2double_rn(lo), -63);
+    const int sh = 64 - __clzll((long long)hi); // significant bits in hi, 1..64
+    const unsigned long long top = sh == 64 ? hi : (hi << (64 - sh)) | (lo >> sh);
+    const unsigned long long rest = sh == 64 ? lo : lo << (64 - sh);
+    return ldexp(__ull2double_rn(top | (rest != 0 ? 1ull : 0ull)), sh - 63);
+}
+
 // Per-echo accumulator limbs -> FP64 echo sums and per-phase collision counts.
 __global__ void noalloc_finish_kernel(const unsigned long long *acc, int K, int n_echoes, int n_phases, double *echo_sum,
                                       unsigned long long *echo_coll)
@@ -67,11 +90,30 @@ __global__ void noalloc_finish_kernel(const unsigned long long *acc, int K, int 
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e <= n_echoes; e += gridDim.x * blockDim.x)
     {
         const unsigned long long *a = acc + (size_t)e * K;
-        // l0 + l1 2^21 + l2 2^42, scaled by 2^-63; each term is exact in FP64
-        const double s = ((double)a[2] * 4398046511104.0 + (double)a[1] * 2097152.0) + (double)a[0];
-        echo_sum[e] = s * 1.0842021724855044e-19;
+        echo_sum[e] = limbs_to_double_rn(a);
         if (echo_coll && e > 0)
             for (int q = 0; q < n_phases; q++) echo_coll[(size_t)(e - 1) * n_phases + q] = a[3 + q];
+    }
+}
+
+// Phase labels of a 3- or 4-phase image (W = 4 words per block: the solid mask, then bit-planes 0-2
+// of the solid voxel's phase index): every solid voxel's index must be below n_phases. The walk
+// reads a phase's table slot from the planes, and an index beyond the caller's phase count would
+// select an unused slot (no relaxation) instead of failing, so such images are reported here.
+__global__ void noalloc_check_labels_kernel(const uint32_t *__restrict__ blocks, int64_t nblocks, int n_phases,
+                                            unsigned *status)
+{
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nblocks; b += (int64_t)gridDim.x * blockDim.x)
+    {
+        const uint4 lo = *reinterpret_cast<const uint4 *>(blocks + b * 8);     // words' low halves
+        const uint4 hi = *reinterpret_cast<const uint4 *>(blocks + b * 8 + 4); // words' high halves
+        uint32_t bad_lo = lo.w, bad_hi = hi.w;                                  // plane 2: index >= 4
+        if (n_phases == 3)
+        {
+            bad_lo |= lo.y & lo.z; // index 3
+            bad_hi |= hi.y & hi.z;
+        }
+        if ((bad_lo & lo.x) | (bad_hi & hi.x)) atomicOr(status, rwnmr::kStatusBadLabel);
     }
 }
 
@@ -128,6 +170,8 @@ extern "C" rwnmr_status rwnmr_cpmg_run_noalloc(const rwnmr_cpmg_params *p, const
                                                      !a->z || !a->seed || !a->collisions)))
         return say(err, errlen, RWNMR_ERR_INVALID, "a required device pointer is NULL");
 
+    if (((uintptr_t)a->blocks & (a->n_phases > 1 ? 15 : 7)) != 0)
+        return say(err, errlen, RWNMR_ERR_INVALID, "blocks must be %d-byte aligned", a->n_phases > 1 ? 16 : 8);
     const int slots = a->n_phases <= 1 ? 1 : (a->n_phases == 2 ? 2 : 4);
     const int K = 3 + slots;
     const int64_t nmax = (int64_t)p->n_echoes * p->steps_per_echo;
@@ -156,6 +200,14 @@ extern "C" rwnmr_status rwnmr_cpmg_run_noalloc(const rwnmr_cpmg_params *p, const
 
     NA_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), s), "status reset");
     NA_CUDA(cudaMemsetAsync(acc, 0, acc_words * 8, s), "accumulator reset");
+    if (slots == 4)
+    {
+        const int64_t nblocks = (int64_t)((a->nx + 3) / 4) * ((a->ny + 3) / 4) * ((a->nz + 3) / 4);
+        const unsigned grid = (unsigned)std::min<int64_t>((nblocks + 255) / 256, 152 * 8);
+        noalloc_check_labels_kernel<<<grid, 256, 0, s>>>(reinterpret_cast<const uint32_t *>(a->blocks), nblocks,
+                                                         a->n_phases, status);
+        NA_CUDA(cudaGetLastError(), "label check kernel");
+    }
     const double *f = p->dfactor;
     noalloc_tables_kernel<<<1, 32, 0, s>>>(tab, slots, a->n_phases, nmax + 1, f[0], a->n_phases > 1 ? f[1] : 1.0,
                                            a->n_phases > 2 ? f[2] : 1.0, a->n_phases > 3 ? f[3] : 1.0);
@@ -213,6 +265,9 @@ extern "C" rwnmr_status rwnmr_cpmg_run_noalloc(const rwnmr_cpmg_params *p, const
     unsigned h = 0;
     NA_CUDA(cudaMemcpyAsync(&h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "status readback");
     NA_CUDA(cudaStreamSynchronize(s), "stream synchronize");
+    if (h & kStatusBadLabel)
+        return say(err, errlen, RWNMR_ERR_INVALID, "a solid voxel's phase index is not below n_phases = %d",
+                   a->n_phases);
     if (h & kStatusBadStart) return say(err, errlen, RWNMR_ERR_INVALID, "a walker starts outside the image");
 #undef NA_CUDA
     return say(err, errlen, RWNMR_OK, "");
