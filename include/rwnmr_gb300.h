@@ -293,8 +293,12 @@ const char *rwnmr_batch_last_error(const rwnmr_batch *batch);
 
 /* Asks the persistent batch walk in flight on batch (or the next one to start) to stop: its CTAs take
  * no further work items, the kernel ends normally, and the call returns RWNMR_ERR_CANCELLED with no
- * results (stored histograms are dropped); later calls run normally. Safe to call from another host
- * thread while a batch call runs. No counterpart in the reference. */
+ * results (stored histograms are dropped); later calls run normally. The request belongs to the batch
+ * call (rwnmr_batch_cpmg / rwnmr_batch_autotune) in flight when it is made, or to the next one if none
+ * is, and that call consumes it when it returns even if no walk saw it (it landed after the last work
+ * item was taken, or the call only evaluated stored histograms): a request never carries over to a
+ * later call. Safe to call from another host thread while a batch call runs. No counterpart in the
+ * reference. */
 rwnmr_status rwnmr_batch_cancel(rwnmr_batch *batch);
 
 /* Time budget of each persistent batch walk launch, in seconds (0, the default: none). A CTA that has

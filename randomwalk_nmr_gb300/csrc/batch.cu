@@ -900,6 +900,19 @@ rwnmr_status histogram_walk(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, in
     return RWNMR_OK;
 }
 
+// A cancel request belongs to the batch call in flight when it is made, or to the next call if
+// none is: every call consumes it when it returns, whether or not one of its walks saw it (the
+// request may land after the last work item was taken, or in a call that walks nothing), so it
+// never carries over into a later, unrelated call.
+struct ConsumeCancel
+{
+    rwnmr_batch *b;
+    ~ConsumeCancel()
+    {
+        if (b && b->h_cancel) __atomic_store_n(b->h_cancel, 0, __ATOMIC_SEQ_CST);
+    }
+};
+
 rwnmr_status check_params(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p)
 {
     if (!p) return put(b->err, RWNMR_ERR_INVALID, "params is NULL");
@@ -1036,6 +1049,7 @@ rwnmr_status rwnmr_batch_cpmg(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, 
         ~Pop() { nvtxRangePop(); }
     } pop;
     if (!b) return RWNMR_ERR_INVALID;
+    ConsumeCancel consume{b};
     rwnmr_status st = check_params(b, p);
     if (st != RWNMR_OK) return st;
     if (!dfactor) return put(b->err, RWNMR_ERR_INVALID, "dfactor is NULL");
@@ -1115,6 +1129,7 @@ rwnmr_status rwnmr_batch_autotune(rwnmr_batch *b, const rwnmr_batch_cpmg_params 
                                   int32_t *best_walkers_per_thread, double *best_ms)
 {
     if (!b) return RWNMR_ERR_INVALID;
+    ConsumeCancel consume{b};
     rwnmr_status st = check_params(b, p);
     if (st != RWNMR_OK) return st;
     const int ni = (int)b->images.size();

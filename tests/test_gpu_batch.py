@@ -161,3 +161,18 @@ def test_batch_cancel_and_time_budget(method):
     got = b.cpmg(f, 40, 3, method=method)
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
     b.close()
+
+
+def test_batch_cancel_does_not_carry_over():
+    """A cancel request made while no walk can see it -- here before a call that only evaluates the
+    stored collision histograms -- is consumed when that call returns: the call succeeds and the
+    next call, which walks again, is not cancelled."""
+    f = dfactor(np.linspace(2.0, 50.0, 16))[None, :].repeat(4, axis=0)
+    b = _big_batch()
+    ref = b.cpmg(f, 40, 3, method="histograms")  # walks and stores the histograms
+    b.cancel()
+    got = b.cpmg(f, 40, 3, method="histograms")  # evaluates only: completes normally
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    again = b.cpmg(f, 40, 3, method="walk")  # walks: must not see the earlier request
+    assert np.array_equal(again[0], ref[0]) and np.array_equal(again[1], ref[1])
+    b.close()
