@@ -12,10 +12,14 @@ Reported:
              engine's stream; L2 flushed before every timed step by writing a 512 MB buffer)
   e2e        the same metric through the C ABI from pinned host buffers: image labels and walker
              initial state copied host->device, echo train and per-echo collisions copied back
-  roofline   achieved gather bytes of the dominant kernel against the measured HBM copy peak, plus
-             the integer-issue bound (warp-instructions per walker-step from an ncu capture)
+  roofline   the instruction-issue bound that binds: algorithmic warp-instructions (48 int32 slots =
+             1.5 per walker-step) per launch / launch time, against SMs x 4 schedulers x the sampled
+             SM clock; the kernel's measured instruction count (ncu) beside it; the gathered bytes
+             against the HBM copy peak as a secondary entry
   cpu_baseline  the oracle's CPU walk (port of the reference's Walker::walk) on a bounded walker
              sample with all host threads
+  rho_fit_batch  (default workload) GPU-seconds of the batched relaxivity fit over 64 uneven images
+             against per-image plain CPMG + the restated GA, the GA run on every image
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload NAME]
   workloads: cpmg-2phase-400 (default), cpmg-1phase-100, cpmg-2phase-small, map-400, pfgse-256[-small],
@@ -148,6 +152,47 @@ def measured_peaks():
         return FALLBACK_HBM_GBS, "fallback", {}
 
 
+# Algorithmic integer work of one walker step, in 32-thread warp-instructions: about 48 int32
+# issue slots (xorshift64 ~12, mod 6 ~8, move and border select ~8, block and bit index ~12, bit
+# test ~4, collision count and position select ~4), i.e. 1.5 warp-instructions per walker-step.
+ALG_WARP_INST_PER_STEP = 48 / 32
+
+
+def kernel_counters(name):
+    """ncu counters of a workload's walk kernel, committed beside its profile summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "kernel_counters.json")) as fh:
+            return json.load(fh).get(name, {})
+    except Exception:
+        return {}
+
+
+def issue_roofline(rate, steps_per_launch, launch_s, device, clocks, peaks, counters):
+    """Instruction-issue roofline of the walk kernel, the bound that binds: achieved = algorithmic
+    warp-instructions per launch / the launch's average device time; peak = SMs (from the device) x 4
+    warp schedulers x the SM clock sampled during the timed region (one warp-instruction each per
+    cycle). The measured instruction count of the kernel (an ncu capture) is reported beside it."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = float(clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0))
+    peak = sms * 4 * mhz * 1e6 / 1e9
+    achieved = ALG_WARP_INST_PER_STEP * steps_per_launch / launch_s / 1e9
+    out = {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gwarp-inst/s", "frac": achieved / peak,
+           "traffic": counters.get("dram_bytes_per_launch"), "traffic_unit": "DRAM bytes per launch (ncu)",
+           "alg_warp_inst_per_walker_step": ALG_WARP_INST_PER_STEP, "walker_steps_per_launch": steps_per_launch,
+           "launch_ms": launch_s * 1e3, "sm_count": sms, "sm_mhz": mhz,
+           "peak_source": "SM count (cudaDevAttrMultiProcessorCount) x 4 schedulers x median sampled SM clock"}
+    if counters.get("warp_inst_per_walker_step"):
+        inst = counters["warp_inst_per_walker_step"]
+        out["measured"] = {"warp_inst_per_walker_step": inst, "issue_active_pct": counters.get("issue_active_pct"),
+                           "l1_hit_pct": counters.get("l1_hit_pct"),
+                           "frac_of_issue_peak": inst * rate / 1e9 / peak,
+                           "source": "ncu smsp__inst_executed.sum, " + counters.get("source", "profiles/") +
+                                     (", " + counters["date"] if counters.get("date") else "")}
+    return out
+
+
 def cpu_baseline(labels, n_phases, walkers, spe, echoes, f, bc, target_s=15.0):
     """The oracle port of the reference's CPU walk on a bounded walker sample, all host threads."""
     from oracle.pyoracle import Oracle, build
@@ -156,17 +201,15 @@ def cpu_baseline(labels, n_phases, walkers, spe, echoes, f, bc, target_s=15.0):
     o = Oracle()
     threads = os.cpu_count() or 1
     x, y, z, s = walkers
-    # calibrate on a small sample, then size the timed sample to ~target_s; a one-echo call measures
-    # the per-call fixed cost (image packing), which the rate must not include
+    # calibrate on a small sample, then size the timed sample to ~target_s; the first call packs the
+    # image, which the oracle keeps for the later calls, so neither timed call includes it
     n0 = min(len(x), 256 * threads)
     e0 = min(echoes, 2000)
     small = (x[:n0], y[:n0], z[:n0], s[:n0])
-    t0 = time.perf_counter()
     o.cpmg(labels, small, 1, spe, f, bc=bc, n_phases=n_phases, threads=threads)
-    fixed = time.perf_counter() - t0
     t0 = time.perf_counter()
     o.cpmg(labels, small, e0, spe, f, bc=bc, n_phases=n_phases, threads=threads)
-    rate = n0 * e0 * spe / max(time.perf_counter() - t0 - fixed, 1e-3)
+    rate = n0 * e0 * spe / max(time.perf_counter() - t0, 1e-3)
     n = int(max(threads * 4, min(len(x), rate * target_s / (echoes * spe))))
     sample = (x[:n], y[:n], z[:n], s[:n])
     t0 = time.perf_counter()
@@ -176,17 +219,45 @@ def cpu_baseline(labels, n_phases, walkers, spe, echoes, f, bc, target_s=15.0):
                 sample=f"first {n} of {len(x)} walkers, all {echoes} echoes x {spe} steps ({dt:.1f} s)"), out, sample
 
 
-def run_reference(args, w):
-    """Reference arm: the reference's CPU walk (oracle port on the GPU machine) on a bounded sample."""
+def oracle_inputs(w):
+    """The workload's image and walkers from the oracle's own restatements of the sphere-pack
+    generator and of the reference's random placement: the reference arm loads no product code."""
     from oracle.pyoracle import Oracle, build
 
+    build(with_ref=False)
+    o = Oracle()
+    labels, por = o.synth_spheres(w["shape"], w["rmin"], w["rmax"], w["porosity"], w["n_phases"], w["img_seed"])
+    x, y, z, s, _ = o.place_walkers(labels, w["walkers"], w["seed"])
+    return o, labels, por, (x, y, z, s)
+
+
+def serial_reference_timing(o, labels, walkers, n_phases, spe, echoes, f, bc, target_s=5.0):
+    """The reference's own CPU order (NMR_cpmg::image_simulation_omp is serial: its OpenMP pragmas are
+    commented out, NMR_cpmg.cpp:209,220) on one core: the oracle's walk with one thread on a walker
+    sample sized to about target_s seconds."""
+    x, y, z, s = walkers
+    n0 = min(len(x), 64)
+    e0 = min(echoes, 2000)
+    o.cpmg(labels, (x[:1], y[:1], z[:1], s[:1]), 1, spe, f, bc=bc, n_phases=n_phases, threads=1)  # packs the image
+    t0 = time.perf_counter()
+    o.cpmg(labels, (x[:n0], y[:n0], z[:n0], s[:n0]), e0, spe, f, bc=bc, n_phases=n_phases, threads=1)
+    rate = n0 * e0 * spe / max(time.perf_counter() - t0, 1e-3)
+    n = int(max(8, min(len(x), rate * target_s / (echoes * spe))))
+    t0 = time.perf_counter()
+    o.cpmg(labels, (x[:n], y[:n], z[:n], s[:n]), echoes, spe, f, bc=bc, n_phases=n_phases, threads=1)
+    dt = time.perf_counter() - t0
+    return dict(value=n * echoes * spe / dt, unit="walker-steps/s", cores=1, kind="port",
+                sample=f"first {n} of {len(x)} walkers, all {echoes} echoes x {spe} steps, one thread ({dt:.1f} s)")
+
+
+def run_reference(args, w):
+    """Reference arm: the reference's CPU walk (oracle port on the GPU machine) on a bounded sample, its
+    inputs from the oracle's own generator and placement (no product code is loaded)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     res, spe, f = derived(w)
-    labels, por, walkers = build_inputs(w)
-    build(with_ref=False)
-    o = Oracle()
+    o, labels, por, walkers = oracle_inputs(w)
     threads = os.cpu_count() or 1
     x, y, z, s = walkers
     n = int(os.environ.get("RWNMR_REF_SAMPLE", "0")) or min(len(x), 8 * threads * 64)
@@ -201,13 +272,15 @@ def run_reference(args, w):
         times.append(time.perf_counter() - t0)
     per = statistics.mean(times)
     value = n * echoes * spe / per
+    serial = serial_reference_timing(o, labels, walkers, w["n_phases"], spe, echoes, f, w["bc"])
     line = {"metric": "walker-steps/s (plain CPMG)", "value": value, "unit": "walker-steps/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+u64 walk, f64 energy",
             "data": "synthetic", "config": {"workload": w["name"], "walkers_timed": n, "echoes": echoes,
                                             "steps_per_echo": spe},
             "cpu_baseline": {"value": value, "unit": "walker-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"first {n} of {len(x)} walkers, all {echoes} echoes per step"},
+                             "sample": f"first {n} of {len(x)} walkers, all {echoes} echoes per step",
+                             "serial": serial},
             "e2e": {"value": value, "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -273,12 +346,16 @@ def run_fit_multiphase(args):
     eng.close()
 
 
-def run_fit_batch(args):
-    """Batched uneven workload: 64 sphere packs with edges U[64, 320], walkers
-    U[1e4, 5e5], 16 relaxivity candidates per image, 3000 echoes of 3 steps: one persistent histogram
-    walk (autotuned block shape) keeps every image's per-echo collision histograms, then each fit
-    iteration evaluates all candidates and derivatives from them (CUDA graph); vs per-image plain
-    CPMG + the restated GA."""
+def fit_batch(args, small=False):
+    """Batched uneven workload: 64 sphere packs with edges U[64, 320] (radii 3-15, porosity U[0.15,
+    0.40], seeds 100-163), walkers U[1e4, 5e5], 16 relaxivity candidates per image, 3000 echoes of 3
+    steps: one persistent histogram walk (autotuned block shape) keeps every image's per-echo collision
+    histograms, then each Gauss-Newton iteration evaluates every candidate and its derivative from them
+    (CUDA graph). Compared with per-image plain CPMG + the restated GA (population 64), run on every
+    image for `args.ga_generations_measured` generations and scaled to `args.ga_generations`: the GPU
+    time of the initial population plus that many times the measured per-generation time (diversity
+    resets, which add evaluations, are not counted, so the GA figure is a lower bound). A full GA run
+    on the smallest image gives the GA's accuracy. Returns the result dict."""
     from concurrent.futures import ThreadPoolExecutor
 
     from randomwalk_nmr_gb300 import Batch, Engine
@@ -286,7 +363,6 @@ def run_fit_batch(args):
     from randomwalk_nmr_gb300.fit import decrease_factor, fit_rho_batch
     from randomwalk_nmr_gb300.ga import GeneticAlgorithm, misfit_fitness
 
-    small = args.workload.endswith("-small")
     n_img = 8 if small else 64
     n_use = min(args.images or n_img, n_img)
     echoes, spe, t2b = args.echoes or (300 if small else 3000), 3, 2800.0
@@ -321,34 +397,49 @@ def run_fit_batch(args):
     fit = fit_rho_batch(b, targets, nwalk, echoes, spe, t2b, rho0, iters=args.fit_iters, method=args.batch_method)
     hist_walk_s = b.histogram_walk_ms * 1e-3 if args.batch_method != "walk" else 0.0
     steps_per_pass = int(nwalk.sum()) * echoes * spe
-    # plain per-image CPMG: one walk per image per GA evaluation
+    b.close()
+
+    # per-image plain CPMG + GA: every image's GA runs on the GPU walk of that image
     eng = Engine(0)
-    per_image_s = []
-    for lab, blocks, w, por in imgs:
+    g_meas = max(1, args.ga_generations_measured)
+    init_s, gen_s, evals_init, evals_gen = 0.0, 0.0, 0, 0
+    for k, (lab, blocks, w, por) in enumerate(imgs):
         eng.upload_labels(lab, 1)
         eng.upload_walkers(*w)
-        eng.cpmg(echoes, spe, 0.999)
-        per_image_s.append(eng.last_kernel_ms * 1e-3)
-    # GA evaluation count from one full GA run on the smallest image
+        spent = [0.0]
+
+        def model(g, k=k):
+            m = eng.cpmg(echoes, spe, decrease_factor(g[0]))["echo_sum"]
+            spent[0] += eng.last_kernel_ms * 1e-3
+            return m / nwalk[k] * bulk
+
+        ga = GeneticAlgorithm(misfit_fitness(model, targets[k], 1e-3), [2.0], [50.0], population=64, seed=5 + k)
+        init_s += spent[0]
+        evals_init += ga.evaluations
+        spent[0] = 0.0
+        e0 = ga.evaluations
+        ga.run(g_meas)
+        gen_s += spent[0]
+        evals_gen += ga.evaluations - e0
+    ga_gpu = init_s + gen_s / g_meas * args.ga_generations
+    # a full GA run on the smallest image: its evaluation count and accuracy
     k0 = int(np.argmin(nwalk * np.array([im[0].size for im in imgs])))
     lab, blocks, w, por = imgs[k0]
     eng.upload_labels(lab, 1)
     eng.upload_walkers(*w)
+    full_s = [0.0]
 
-    def model(g):
+    def model0(g):
         m = eng.cpmg(echoes, spe, decrease_factor(g[0]))["echo_sum"]
+        full_s[0] += eng.last_kernel_ms * 1e-3
         return m / nwalk[k0] * bulk
 
-    ga = GeneticAlgorithm(misfit_fitness(model, targets[k0], 1e-3), [2.0], [50.0], population=64, seed=5)
-    ga.run(args.ga_generations)
-    ga_gpu = float(np.sum(per_image_s)) * ga.evaluations
-    line = {"metric": "GPU-seconds of the relaxivity fit over uneven images (batched+adjoint vs per-image CPMG+GA)",
-            "value": fit["gpu_seconds"], "unit": "GPU-s", "higher_is_better": False, "impl": "gb300",
-            "config": {"workload": args.workload, "images": n_img, "walkers_total": int(nwalk.sum()),
-                       "echoes": echoes, "steps_per_echo": spe, "candidates": 16,
-                       "walker_steps_per_pass": steps_per_pass, "autotuned_threads": tuned, "autotuned_walkers_per_thread": tuned_wpt,
-                       "autotune_best_walk_ms": tune_ms,
-                       "setup_seconds": setup_s},
+    ga0 = GeneticAlgorithm(misfit_fitness(model0, targets[k0], 1e-3), [2.0], [50.0], population=64, seed=5)
+    ga0.run(args.ga_generations)
+    eng.close()
+    return {"images": n_img, "walkers_total": int(nwalk.sum()), "echoes": echoes, "steps_per_echo": spe,
+            "candidates": 16, "walker_steps_per_pass": steps_per_pass, "autotuned_threads": tuned,
+            "autotuned_walkers_per_thread": tuned_wpt, "autotune_best_walk_ms": tune_ms, "setup_seconds": setup_s,
             "batched_fit": {"gpu_seconds": fit["gpu_seconds"], "passes": fit["walks"],
                             "method": "walk" if args.batch_method == "walk" else "histograms",
                             "histogram_walk_seconds": hist_walk_s,
@@ -359,15 +450,32 @@ def run_fit_batch(args):
                                                                   steps_per_pass * fit["walks"] / fit["gpu_seconds"]),
                             "max_abs_rho_error": float(np.max(np.abs(fit["rho"] - hidden))),
                             "median_abs_rho_error": float(np.median(np.abs(fit["rho"] - hidden)))},
-            "per_image_cpmg_ga": {"gpu_seconds_estimate": ga_gpu, "plain_walk_gpu_seconds_all_images":
-                                  float(np.sum(per_image_s)), "ga_evaluations_per_image": ga.evaluations,
-                                  "ga_generations": args.ga_generations, "population": 64,
-                                  "note": "GA GPU time = measured plain CPMG walk time of every image x the "
-                                          "evaluation count of a full GA run on the smallest image"},
+            "per_image_cpmg_ga": {"gpu_seconds": ga_gpu, "measured_gpu_seconds": init_s + gen_s,
+                                  "initial_population_gpu_seconds": init_s, "initial_population_evaluations": evals_init,
+                                  "measured_generations": g_meas, "measured_generation_gpu_seconds": gen_s,
+                                  "measured_generation_evaluations": evals_gen, "generations": args.ga_generations,
+                                  "population": 64,
+                                  "method": (f"GA run on every image for {g_meas} generation(s) on that image's GPU "
+                                             f"walk; GPU time = initial population + {args.ga_generations} x the "
+                                             "measured per-generation time (diversity resets not counted: a lower "
+                                             "bound)"),
+                                  "full_run_smallest_image": {"generations": args.ga_generations,
+                                                              "evaluations": ga0.evaluations,
+                                                              "gpu_seconds": full_s[0],
+                                                              "abs_rho_error": float(abs(ga0.best[0][0] - hidden[k0])),
+                                                              "batched_fit_abs_rho_error":
+                                                                  float(abs(fit["rho"][k0] - hidden[k0]))}},
             "gpu_seconds_ratio_ga_over_batched": ga_gpu / max(fit["gpu_seconds"], 1e-12)}
+
+
+def run_fit_batch(args):
+    r = fit_batch(args, args.workload.endswith("-small"))
+    line = {"metric": "GPU-seconds of the relaxivity fit over uneven images (batched+adjoint vs per-image CPMG+GA)",
+            "value": r["batched_fit"]["gpu_seconds"], "unit": "GPU-s", "higher_is_better": False, "impl": "gb300",
+            "config": dict({k: v for k, v in r.items() if not isinstance(v, dict)}, workload=args.workload)}
+    line.update({k: v for k, v in r.items() if isinstance(v, dict)})
+    line["gpu_seconds_ratio_ga_over_batched"] = r["gpu_seconds_ratio_ga_over_batched"]
     print(json.dumps(line))
-    eng.close()
-    b.close()
 
 
 def pfgse_setup(small, direction=(0.0, 0.0, 1.0)):
@@ -402,11 +510,7 @@ def run_pfgse(args):
         # reference arm: the reference's CPU PFGSE walk and phase sums (oracle port) on a bounded sample
         if int(os.environ.get("RANK", "0")) != 0:
             return
-        from oracle.pyoracle import Oracle, build
-
-        labels, por, walkers = build_inputs(w)
-        build(with_ref=False)
-        o = Oracle()
+        o, labels, por, walkers = oracle_inputs(w)
         threads = os.cpu_count() or 1
         m = min(len(walkers[0]), 64 * 1024)
         sample = tuple(a[:m] for a in walkers)
@@ -472,6 +576,12 @@ def run_pfgse(args):
                "d2h_bytes_per_step": int(out["M"].nbytes + out["esum"].nbytes + out["msd"].nbytes), "ms_per_step": te * 1e3}
     peak, peak_kind, peaks = measured_peaks()
     achieved = steps_per_run * 4 / t_step / 1e9
+    clk_sum = clk.summary()
+    roofline = issue_roofline(value, steps_per_run, t_step, local, clk_sum, peaks, kernel_counters(w["name"]))
+    roofline["note"] = ("one launch walks every walker to the longest exposure time; its time includes the "
+                        "displacement-histogram and phase kernels")
+    roofline["hbm"] = {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "peak_source": peak_kind, "note": "4 B bit-block half gathered per walker-step; L2/L1-resident"}
     base, err = None, None
     if not args.no_cpu_baseline:
         from oracle.pyoracle import Oracle, build
@@ -507,12 +617,9 @@ def run_pfgse(args):
                        "exposure_times_ms": [round(float(d), 4) for d in deltas],
                        "steps": [int(v) for v in steps], "walker_steps_per_step": steps_per_run,
                        "l2": "flushed (512 MB write) before every timed step", "parallelism": "1 GPU"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "peak_source": peak_kind,
-                         "note": "achieved = 4 B bit-block half gathered per walker-step / walk time; L2-resident image, "
-                                 "issue-bound like the CPMG walk"},
+            "roofline": roofline,
             "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
-            "attenuation_max_err_vs_oracle": err, "clocks": clk.summary(),
+            "attenuation_max_err_vs_oracle": err, "clocks": clk_sum,
             "check": {"M0_equals_energy_sum": bool(np.allclose(out["M"][:, 0], out["esum"], rtol=1e-12))}}
     print(json.dumps(line))
     eng.close()
@@ -530,6 +637,10 @@ def main():
     ap.add_argument("--ga-generations", type=int, default=50)
     ap.add_argument("--fit-evals", type=int, default=40)
     ap.add_argument("--fit-iters", type=int, default=6)
+    ap.add_argument("--ga-generations-measured", type=int, default=1,
+                    help="rho-fit-batch: GA generations actually run on every image (scaled to --ga-generations)")
+    ap.add_argument("--no-fit", action="store_true",
+                    help="default workload: skip the batched relaxivity fit carried in the bench line")
     ap.add_argument("--echoes", type=int, default=0, help="rho-fit-batch: echo count override (profiling)")
     ap.add_argument("--gradient-direction", default="0,0,1",
                     help="pfgse workloads: gradient direction x,y,z (an oblique one takes the general phase path)")
@@ -657,33 +768,17 @@ def main():
     words = 1 if w["n_phases"] == 1 else (2 if w["n_phases"] == 2 else 4)
     gather_bytes = 4 * words  # algorithmic bytes gathered per walker-step: one 32-bit half of each block word
     launches_per_walk = max(1, launches // max(1, args.steps))
-    achieved = steps_per_run * gather_bytes / t_step / 1e9
-    counters = {}
-    try:
-        with open(os.path.join(ROOT, "profiles", "kernel_counters.json")) as fh:
-            counters = json.load(fh).get(w["name"], {})
-    except Exception:
-        pass
+    counters = kernel_counters(w["name"])
     clk_sum = clk.summary()
-    sm_hz = float(clk_sum.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
-    issue_peak = 152 * 4 * sm_hz  # warp-instructions per second (4 schedulers per SM)
-    inst = counters.get("warp_inst_per_walker_step")
-    cache = ""
-    if counters.get("l1_hit_pct") is not None and counters.get("dram_bytes_per_launch"):
-        cache = " (ncu: %.1f%% L1 hit, %.0f MB DRAM per launch)" % (counters["l1_hit_pct"],
-                                                                   counters["dram_bytes_per_launch"] / 1e6)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": counters.get("dram_bytes_per_launch"), "traffic_unit": "bytes per launch",
-                "launches_per_walk": launches_per_walk, "peak_source": peak_kind,
-                "note": ("achieved = bit-block bytes gathered per walker-step (4 B per block word) x walker-steps / "
-                         "walk-kernel time, against the measured HBM copy peak; the gathers are served on chip"
-                         + cache + ", so the binding roof is instruction issue, reported under 'issue'"
-                         + (" and the FP64 pipe, under 'fp64'" if field else ""))}
-    if inst:
-        ach_issue = (value / world) * inst
-        roofline["issue"] = {"achieved_warp_inst_per_s": ach_issue, "peak_warp_inst_per_s": issue_peak,
-                             "frac": ach_issue / issue_peak, "warp_inst_per_walker_step": inst,
-                             "source": "ncu smsp__inst_executed.sum (profiles/kernel_counters.json)"}
+    roofline = issue_roofline(value / world, steps_per_run / launches_per_walk, t_step / launches_per_walk, local,
+                              clk_sum, peaks, counters)
+    roofline["hbm"] = {"achieved": steps_per_run * gather_bytes / t_step / 1e9, "peak": peak, "unit": "GB/s",
+                       "frac": steps_per_run * gather_bytes / t_step / 1e9 / peak, "peak_source": peak_kind,
+                       "traffic": counters.get("dram_bytes_per_launch"), "traffic_unit": "bytes per launch",
+                       "note": "bit-block bytes gathered per walker-step (4 B per block word) x walker-steps / walk-"
+                               "kernel time, against the measured HBM copy peak; the gathers are served on chip "
+                               "(L1 hits), so this roof does not bind"}
+    roofline["launches_per_walk"] = launches_per_walk
     if field:
         # the reference's phase updates: two FP64 fused multiply-adds per step, kept bit for bit
         roofline["fp64"] = {"dfma_per_walker_step": 2, "achieved_tflops": (value / world) * 2 * 2 / 1e12,
@@ -761,8 +856,13 @@ def main():
                 "clocks": clk_sum}
         if not mapping:
             line["echo_check"] = float(out["echo_sum"][-1] / out["echo_sum"][0])
-        print(json.dumps(line))
     eng.close()
+    if rank == 0:
+        if w["name"] == "cpmg-2phase-400" and world == 1 and not args.no_fit:
+            # the second headline figure: GPU-seconds of the batched relaxivity fit over 64 uneven
+            # images against per-image plain CPMG + GA on the same GPU (the rho-fit-batch workload)
+            line["rho_fit_batch"] = fit_batch(args)
+        print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
 
