@@ -296,9 +296,13 @@ def _sphere_image(args):
 
 
 def run_fit_multiphase(args):
+    print(json.dumps(fit_multiphase(args, args.workload.endswith("-small"), args.workload)))
+
+
+def fit_multiphase(args, small, name):
     """Differentiable CPMG fit of a multi-phase image: 200^3, 4 solid phases, 500k walkers, 5000 echoes
     of 3 steps; L-BFGS with gradients from the walk's forward sensitivities (one walk per evaluation) vs the
-    restated GA (population 64) on the same GPU walk."""
+    restated GA (population 64) on the same GPU walk. Returns the result line."""
     import torch
 
     from randomwalk_nmr_gb300 import Engine
@@ -306,7 +310,6 @@ def run_fit_multiphase(args):
     from randomwalk_nmr_gb300.fit import fit_rho_adjoint
     from randomwalk_nmr_gb300.ga import GeneticAlgorithm, misfit_fitness
 
-    small = args.workload.endswith("-small")
     n, echoes, edge = (50_000, 500, 100) if small else (500_000, 5000, 200)
     lab, blocks, w, por = _sphere_image(((edge, edge, edge), 5.0, 12.0, 0.30, 4, 4, n, 7))
     eng = Engine(0)
@@ -339,7 +342,7 @@ def run_fit_multiphase(args):
     floor = float(np.sum(((clean - target) / scale) ** 2))
     line = {"metric": "GPU-seconds of the relaxivity fit (multi-phase CPMG)", "value": res["gpu_seconds"],
             "unit": "GPU-s", "higher_is_better": False, "impl": "gb300",
-            "config": {"workload": args.workload, "image": f"{edge}^3, 4 phases, porosity {por:.3f}",
+            "config": {"workload": name, "image": f"{edge}^3, 4 phases, porosity {por:.3f}",
                        "walkers": n, "echoes": echoes, "steps_per_echo": spe, "T2b_ms": t2b,
                        "noise_sigma": 1e-3},
             "gradient_fit": {"gpu_seconds": res["gpu_seconds"], "walks": res["walks"], "evals": res["evals"],
@@ -350,8 +353,8 @@ def run_fit_multiphase(args):
                        "wall_seconds": ga_wall},
             "noise_floor_loss": floor,
             "gpu_seconds_ratio_ga_over_gradient": ga_gpu_fit / max(res["gpu_seconds"], 1e-12)}
-    print(json.dumps(line))
     eng.close()
+    return line
 
 
 def fit_batch(args, small=False):
@@ -508,12 +511,12 @@ def pfgse_setup(small, direction=(0.0, 0.0, 1.0)):
 
 
 def run_pfgse(args):
-    import torch
-
-    from randomwalk_nmr_gb300 import Engine
-
     direction = tuple(float(v) for v in args.gradient_direction.split(","))
-    w, res, steps, kvec, f, deltas = pfgse_setup(args.workload.endswith("-small"), direction)
+    small = args.workload.endswith("-small")
+    if args.impl != "reference":
+        print(json.dumps(pfgse_measure(args, small, direction)))
+        return
+    w, res, steps, kvec, f, deltas = pfgse_setup(small, direction)
     if args.impl == "reference":
         # reference arm: the reference's CPU PFGSE walk and phase sums (oracle port) on a bounded sample
         if int(os.environ.get("RANK", "0")) != 0:
@@ -539,6 +542,15 @@ def run_pfgse(args):
                                            "sample": f"first {m} walkers, all 10 exposure times"},
                           "e2e": {"value": v, "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
+
+
+def pfgse_measure(args, small, direction):
+    """The PFGSE workload on the GPU (see pfgse_setup); returns the result line."""
+    import torch
+
+    from randomwalk_nmr_gb300 import Engine
+
+    w, res, steps, kvec, f, deltas = pfgse_setup(small, direction)
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     labels, por, walkers = build_inputs(w)
@@ -629,8 +641,8 @@ def run_pfgse(args):
             "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
             "attenuation_max_err_vs_oracle": err, "clocks": clk_sum,
             "check": {"M0_equals_energy_sum": bool(np.allclose(out["M"][:, 0], out["esum"], rtol=1e-12))}}
-    print(json.dumps(line))
     eng.close()
+    return line
 
 
 def main():
@@ -648,7 +660,7 @@ def main():
     ap.add_argument("--ga-generations-measured", type=int, default=1,
                     help="rho-fit-batch: GA generations actually run on every image (scaled to --ga-generations)")
     ap.add_argument("--no-fit", action="store_true",
-                    help="default workload: skip the batched relaxivity fit carried in the bench line")
+                    help="default workload: skip the other configurations carried in the bench line (fits, PFGSE)")
     ap.add_argument("--echoes", type=int, default=0, help="rho-fit-batch: echo count override (profiling)")
     ap.add_argument("--gradient-direction", default="0,0,1",
                     help="pfgse workloads: gradient direction x,y,z (an oblique one takes the general phase path)")
@@ -870,6 +882,10 @@ def main():
             # the second headline figure: GPU-seconds of the batched relaxivity fit over 64 uneven
             # images against per-image plain CPMG + GA on the same GPU (the rho-fit-batch workload)
             line["rho_fit_batch"] = fit_batch(args)
+            # the other benchmark configurations measured in the same run: the PFGSE diffusion walk
+            # (256^3, 64 gradients x 10 exposure times) and the differentiable multi-phase fit
+            line["pfgse_256"] = pfgse_measure(args, False, (0.0, 0.0, 1.0))
+            line["rho_fit_multiphase"] = fit_multiphase(args, False, "rho-fit-multiphase")
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
