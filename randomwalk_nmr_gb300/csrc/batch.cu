@@ -39,6 +39,9 @@ namespace
 {
 constexpr int kCand = 16;             // candidate slots per image
 constexpr int kWin = 16;              // echoes per shared-memory window
+// an image gets a Morton copy (and its walkers the Morton step) when the copy takes at most this much,
+// whatever the padding: only the image's own voxels are ever read, so padding costs memory, not cache
+constexpr uint64_t kBatchMortonBytes = 64ull << 20;
 constexpr double kEScale = 144115188075855872.0; // 2^57: energy scale (2 walkers x 32 lanes sum below 2^63)
 constexpr int kScaleBits = 57;
 constexpr unsigned FULLM = 0xffffffffu;
@@ -328,27 +331,33 @@ __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
         __syncthreads();
         unsigned *H = L.hist + img.hist0;
         const int spe = L.steps_per_echo;
-        int64_t row = 0; // hist_row(e), stepped: row(e + 1) = row(e) + spe * e + 1
-        for (int e = 0; e <= L.n_echoes; row += (int64_t)spe * e + 1, e++)
-        {
+        // the echo loop for one step kind, chosen once per work item
+        auto walk_item = [&](auto morton) __attribute__((always_inline)) {
+            constexpr bool MORT = decltype(morton)::value;
+            int64_t row = 0; // hist_row(e), stepped: row(e + 1) = row(e) + spe * e + 1
+            for (int e = 0; e <= L.n_echoes; row += (int64_t)spe * e + 1, e++)
+            {
 #pragma unroll
-            for (int j = 0; j < WPT; j++)
-                if (active[j])
-                {
-                    if (e > 0)
-                        for (int s = 0; s < spe; s++)
-                        {
-                            bool wall;
-                            int ph;
-                            if (mort)
-                                morton_step<1>(img.mi, sdir, P[j], seed[j], wall, ph);
-                            else
-                                walker_step<BC, 1>(im, p[j], seed[j], wall, ph);
-                            c[j] += wall ? 1u : 0u;
-                        }
-                    atomicAdd(H + row + c[j], 1u);
-                }
-        }
+                for (int j = 0; j < WPT; j++)
+                    if (active[j])
+                    {
+                        if (e > 0)
+                            for (int s = 0; s < spe; s++)
+                            {
+                                bool wall;
+                                int ph;
+                                if (MORT)
+                                    morton_step<1>(img.mi, sdir, P[j], seed[j], wall, ph);
+                                else
+                                    walker_step<BC, 1>(im, p[j], seed[j], wall, ph);
+                                c[j] += wall ? 1u : 0u;
+                            }
+                        atomicAdd(H + row + c[j], 1u);
+                    }
+            }
+        };
+        if (BC == BC_NOFLUX && mort) walk_item(std::true_type{});
+        else walk_item(std::false_type{});
     }
 }
 
@@ -641,7 +650,7 @@ rwnmr_status upload(rwnmr_batch *b, int n_echoes, int spe)
         size_t total = 0;
         for (int k = 0; k < ni; k++)
         {
-            b->images[k].mi = morton_params(b->images[k].nx, b->images[k].ny, b->images[k].nz, words[k]);
+            b->images[k].mi = morton_params(b->images[k].nx, b->images[k].ny, b->images[k].nz, words[k], 1, kBatchMortonBytes);
             total += words[k];
         }
         if (total)
