@@ -296,7 +296,9 @@ __global__ void __launch_bounds__(512, 2) batch_cpmg_kernel(BatchLaunch L)
 //   sum_w f^c_w(e) = sum_c H[e][c] f^c   (batch_eval_kernel).
 // The increments are fire-and-forget atomics; the rows a CTA is filling (its walkers share the
 // echo) stay in L2.
-template <int BC, int WPT>
+// SPE: steps per echo fixed at compile time (1-3, one walker per thread), so the step loop unrolls;
+// 0 reads it from the launch.
+template <int BC, int WPT, int SPE = 0>
 __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
 {
     __shared__ int s_item;
@@ -330,7 +332,7 @@ __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
         }
         __syncthreads();
         unsigned *H = L.hist + img.hist0;
-        const int spe = L.steps_per_echo;
+        const int spe = SPE ? SPE : L.steps_per_echo;
         // the echo loop for one step kind, chosen once per work item
         auto walk_item = [&](auto morton) __attribute__((always_inline)) {
             constexpr bool MORT = decltype(morton)::value;
@@ -342,6 +344,7 @@ __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
                     if (active[j])
                     {
                         if (e > 0)
+#pragma unroll(SPE ? SPE : 1)
                             for (int s = 0; s < spe; s++)
                             {
                                 bool wall;
@@ -883,6 +886,9 @@ rwnmr_status histogram_walk(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, in
     auto by_wpt = [&](auto bcc) {
         constexpr int BC = decltype(bcc)::value;
         if (wpt == 2) launch_persistent(b, batch_hist_kernel<BC, 2>, L, block, 0);
+        else if (p->steps_per_echo == 3) launch_persistent(b, batch_hist_kernel<BC, 1, 3>, L, block, 0);
+        else if (p->steps_per_echo == 2) launch_persistent(b, batch_hist_kernel<BC, 1, 2>, L, block, 0);
+        else if (p->steps_per_echo == 1) launch_persistent(b, batch_hist_kernel<BC, 1, 1>, L, block, 0);
         else launch_persistent(b, batch_hist_kernel<BC, 1>, L, block, 0);
     };
     if (p->bc == RWNMR_BC_PERIODIC) by_wpt(std::integral_constant<int, BC_PERIODIC>{});
