@@ -296,8 +296,11 @@ __global__ void __launch_bounds__(512, 2) batch_cpmg_kernel(BatchLaunch L)
 //   sum_w f^c_w(e) = sum_c H[e][c] f^c   (batch_eval_kernel).
 // The increments are fire-and-forget atomics; the rows a CTA is filling (its walkers share the
 // echo) stay in L2.
-// SPE: steps per echo fixed at compile time (1-3, one walker per thread), so the step loop unrolls;
-// 0 reads it from the launch.
+// SPE: steps per echo fixed at compile time (1-3, one walker per thread, noflux), so the step loop
+// unrolls; 0 reads it from the launch. (The periodic instance with 3 steps fixed gave histograms that
+// differ from the candidate walk's for one image of the test batch, deterministically, while the same
+// code with the count read at run time matches; the cause was not found, so the fixed-count instances
+// serve the noflux walk only, where they match bit for bit.)
 template <int BC, int WPT, int SPE = 0>
 __global__ void __launch_bounds__(512) batch_hist_kernel(BatchLaunch L)
 {
@@ -886,9 +889,9 @@ rwnmr_status histogram_walk(rwnmr_batch *b, const rwnmr_batch_cpmg_params *p, in
     auto by_wpt = [&](auto bcc) {
         constexpr int BC = decltype(bcc)::value;
         if (wpt == 2) launch_persistent(b, batch_hist_kernel<BC, 2>, L, block, 0);
-        else if (p->steps_per_echo == 3) launch_persistent(b, batch_hist_kernel<BC, 1, 3>, L, block, 0);
-        else if (p->steps_per_echo == 2) launch_persistent(b, batch_hist_kernel<BC, 1, 2>, L, block, 0);
-        else if (p->steps_per_echo == 1) launch_persistent(b, batch_hist_kernel<BC, 1, 1>, L, block, 0);
+        else if (BC == BC_NOFLUX && p->steps_per_echo == 3) launch_persistent(b, batch_hist_kernel<BC, 1, 3>, L, block, 0);
+        else if (BC == BC_NOFLUX && p->steps_per_echo == 2) launch_persistent(b, batch_hist_kernel<BC, 1, 2>, L, block, 0);
+        else if (BC == BC_NOFLUX && p->steps_per_echo == 1) launch_persistent(b, batch_hist_kernel<BC, 1, 1>, L, block, 0);
         else launch_persistent(b, batch_hist_kernel<BC, 1>, L, block, 0);
     };
     if (p->bc == RWNMR_BC_PERIODIC) by_wpt(std::integral_constant<int, BC_PERIODIC>{});

@@ -307,3 +307,16 @@ def test_checkpoint_and_resume_in_another_context(engine):
     other.close()
     for key in ("x", "y", "z", "seed", "collisions"):
         assert np.array_equal(resumed[key], full[key]), key
+
+
+@pytest.mark.parametrize("bc", ["noflux", "periodic", "mirror"])
+@pytest.mark.parametrize("spe", [1, 2, 3])
+@pytest.mark.parametrize("n_phases", [1, 2])
+def test_cpmg_fixed_step_instances(engine, oracle, bc, spe, n_phases):
+    """The instances with the steps per echo fixed at compile time (1-3), including the Morton walk's
+    fast echo loop (noflux), for every boundary condition, against the oracle; 2600 walkers leave a
+    partial last CTA, so both echo loops run."""
+    lab = image(shape=(27, 31, 23), n_phases=n_phases, seed=17)
+    w = walkers(lab, 2600, 21)
+    g, st, o = run_both(engine, oracle, lab, w, 70, spe, dfactor([7.0, 30.0][:n_phases]), bc=bc, n_phases=n_phases)
+    assert_parity(g, st, o)
