@@ -811,6 +811,34 @@ __global__ void morton_build_kernel(DevImage im, int W, uint32_t n_words, uint32
     if (w >= n_words) return;
     uint32_t acc[4] = {0, 0, 0, 0};
     const uint32_t *base = reinterpret_cast<const uint32_t *>(im.blocks);
+    if ((im.mi.mx & 9u) == 9u && (im.mi.my & 18u) == 18u && (im.mi.mz & 4u) == 4u)
+    {
+        // The five lowest index bits are x0, y0, z0, x1, y1 (the box spans at least 4 x 4 x 2 voxels):
+        // word w is then one half (z & 2) of one bit-block -- the 4 x 4 x 2 voxels at its base corner --
+        // with its bits reordered from the block's x + 4 y + 16 z to the index's x0 y0 z0 x1 y1.
+        const uint32_t P = w << 5;
+        const uint32_t x = undilate_bits(P, im.mi.mx), y = undilate_bits(P, im.mi.my), z = undilate_bits(P, im.mi.mz);
+        if (x < (uint32_t)im.nx && y < (uint32_t)im.ny && z < (uint32_t)im.nz)
+        {
+            const uint32_t blk = (x >> 2) + (y >> 2) * (uint32_t)im.bcols + (z >> 2) * (uint32_t)im.bcr;
+            const uint32_t *bp = base + (size_t)blk * (2 * W) + ((z >> 1) & 1u) * W;
+            for (int k = 0; k < W; k++)
+            {
+                const uint32_t v = bp[k];
+                uint32_t r = 0;
+#pragma unroll
+                for (uint32_t m = 0; m < 32; m++)
+                {
+                    const uint32_t src = (m & 1u) | (((m >> 3) & 1u) << 1) | (((m >> 1) & 1u) << 2) |
+                                         (((m >> 4) & 1u) << 3) | (((m >> 2) & 1u) << 4);
+                    r |= ((v >> src) & 1u) << m;
+                }
+                acc[k] = r;
+            }
+        }
+        for (int k = 0; k < W; k++) out[(size_t)w * W + k] = acc[k];
+        return;
+    }
     for (uint32_t b = 0; b < 32; b++)
     {
         const uint32_t P = (w << 5) | b;
