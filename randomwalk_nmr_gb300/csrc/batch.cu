@@ -396,17 +396,19 @@ __global__ void batch_range_kernel(BatchLaunch L, int n_images)
 // walker by walker, so both paths return identical sums. Exact arithmetic: V is split into 32-bit
 // halves and each half's products h * V_half are summed in u64 (h * 2^32 summed over fewer than
 // 2^31 walkers stays below 2^63); the two sums are stored as the accumulators' lo / hi words.
-// A CTA computes kEvRows echoes x 32 outputs; thread t owns output t % 32 for kEvRows / 8 echoes.
-// Histogram counts and candidate values are staged through shared memory kEvChunk counts at a time.
-constexpr int kEvRows = 32, kEvChunk = 64, kEvThreads = 256;
-constexpr int kEvRowsPerThread = kEvRows / (kEvThreads / 32);
+// A CTA computes kEvRows echoes x 32 outputs with kEvThreads threads: thread t owns the output pair
+// 2 (t % 16), 2 (t % 16) + 1 for the 4 echoes rg .. rg + 3, rg = 4 (t / 16) -- 16 multiply-adds per
+// count from one 16-byte load of its 4 counts and one of its 2 values. Histogram counts and candidate
+// values are staged through shared memory kEvChunk counts at a time.
+constexpr int kEvRows = 32, kEvChunk = 64, kEvThreads = 128;
+constexpr int kEvRowsPerThread = 4;
 
 __global__ void __launch_bounds__(kEvThreads) batch_eval_kernel(BatchLaunch L, int row_blocks)
 {
-    // [c][echo] and [c][output]; one padding column keeps the staging stores (consecutive threads,
-    // consecutive c) off a single bank
-    __shared__ unsigned sh[kEvChunk][kEvRows + 1];
-    __shared__ unsigned long long sv[kEvChunk][2 * kCand + 1];
+    // [c][echo] (rows padded to 36 words: 16-byte aligned, staging stores spread over banks) and
+    // [c][output]
+    __shared__ __align__(16) unsigned sh[kEvChunk][kEvRows + 4];
+    __shared__ __align__(16) unsigned long long sv[kEvChunk][2 * kCand];
     const int img_i = blockIdx.x / row_blocks;
     const int e0 = (blockIdx.x % row_blocks) * kEvRows;
     const BatchImage img = L.images[img_i];
@@ -429,11 +431,12 @@ __global__ void __launch_bounds__(kEvThreads) batch_eval_kernel(BatchLaunch L, i
     }
     __syncthreads();
     const int64_t cmin = s_lo & ~(unsigned)(kEvChunk - 1), cmax = s_hi;
-    const int o = threadIdx.x & 31;
-    const int rg = (threadIdx.x >> 5) * kEvRowsPerThread;
-    unsigned long long lo[kEvRowsPerThread], hi[kEvRowsPerThread];
+    const int op = threadIdx.x & 15;                        // outputs 2 op, 2 op + 1
+    const int rg = (threadIdx.x >> 4) * kEvRowsPerThread;    // echoes e0 + rg .. + 3
+    unsigned long long lo[kEvRowsPerThread][2], hi[kEvRowsPerThread][2];
 #pragma unroll
-    for (int k = 0; k < kEvRowsPerThread; k++) lo[k] = hi[k] = 0;
+    for (int k = 0; k < kEvRowsPerThread; k++)
+        lo[k][0] = lo[k][1] = hi[k][0] = hi[k][1] = 0;
     for (int64_t c0 = cmin; c0 <= cmax; c0 += kEvChunk)
     {
         for (int k = threadIdx.x; k < kEvChunk * kEvRows; k += kEvThreads)
@@ -459,28 +462,37 @@ __global__ void __launch_bounds__(kEvThreads) batch_eval_kernel(BatchLaunch L, i
 #pragma unroll 4
         for (int cc = 0; cc < kEvChunk; cc++)
         {
-            const unsigned long long v = sv[cc][o];
-            const unsigned vl = (unsigned)v, vh = (unsigned)(v >> 32);
+            const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(&sv[cc][2 * op]);
+            const uint4 h = *reinterpret_cast<const uint4 *>(&sh[cc][rg]);
+            const unsigned vl0 = (unsigned)v.x, vh0 = (unsigned)(v.x >> 32);
+            const unsigned vl1 = (unsigned)v.y, vh1 = (unsigned)(v.y >> 32);
+            const unsigned hv[4] = {h.x, h.y, h.z, h.w};
 #pragma unroll
             for (int k = 0; k < kEvRowsPerThread; k++)
             {
-                const unsigned h = sh[cc][rg + k];
-                lo[k] += (unsigned long long)h * vl;
-                hi[k] += (unsigned long long)h * vh;
+                lo[k][0] += (unsigned long long)hv[k] * vl0;
+                hi[k][0] += (unsigned long long)hv[k] * vh0;
+                lo[k][1] += (unsigned long long)hv[k] * vl1;
+                hi[k][1] += (unsigned long long)hv[k] * vh1;
             }
         }
         __syncthreads();
     }
-    if (o >= kCand && !L.deriv) return;
+    if (2 * op >= kCand && !L.deriv) return;
     unsigned long long *acc = L.acc + img.acc0;
 #pragma unroll
     for (int k = 0; k < kEvRowsPerThread; k++)
     {
         const int e = e0 + rg + k;
         if (e > L.n_echoes) break;
-        unsigned long long *a = acc + ((size_t)e * kCand + (o & (kCand - 1))) * 4 + (o >= kCand ? 2 : 0);
-        a[0] = lo[k];
-        a[1] = hi[k];
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+        {
+            const int o = 2 * op + j;
+            unsigned long long *a = acc + ((size_t)e * kCand + (o & (kCand - 1))) * 4 + (o >= kCand ? 2 : 0);
+            a[0] = lo[k][j];
+            a[1] = hi[k][j];
+        }
     }
 }
 

@@ -161,8 +161,118 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
     // -- scattered over the lanes' counts late in a walk -- to a few lanes per warp (looking up every
     // lane every echo measured 25 % slower).
     constexpr bool FAST = MORTON && SPE > 0 && !SENS && !WF;
+    constexpr bool REPLAY = FAST && SPE == 1 && (NP == 1 || PACK);
     bool done = false;
-    if constexpr (FAST)
+    if constexpr (REPLAY)
+    {
+        if (__syncthreads_and(active))
+        {
+            done = true;
+            // One step per echo: during a window of n <= 32 echoes a lane only shifts its collisions
+            // into bit masks (echo j of the window is bit n-1-j of m; the phase-1 ones also of mp).
+            // After the window each lane replays its few collisions in echo order and adds the change
+            // of its three energy limbs, and the collision, into the window's per-echo counters dsum
+            // (shared 32-bit atomics). The flush turns the changes into the CTA's limb sums after each
+            // echo with a prefix sum over the window, starting from the sums after the previous window.
+            // A CTA's limb sums stay below 2^30, so the 32-bit modular arithmetic is exact and the
+            // global counters receive the same integers as from per-echo warp reductions.
+            __shared__ uint32_t dsum[2][32][4]; // [buffer][echo of the window][limb 0-2, collisions]
+            __shared__ uint32_t lsum0[kWalkThreads / 32][3];
+            const int wp = threadIdx.x >> 5;
+            uint32_t lk = 0; // warps 0-2: the CTA's sum of limb wp after the last flushed echo
+            {
+                const uint64_t es = energy_fx<NP>(L.tfx, L.tstride, c);
+                const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(es & M21));
+                const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((es >> 21) & M21));
+                const uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(es >> 42));
+                if (lane == 0)
+                {
+                    lsum0[wp][0] = r0;
+                    lsum0[wp][1] = r1;
+                    lsum0[wp][2] = r2;
+                }
+                for (int k = threadIdx.x; k < 2 * 32 * 4; k += blockDim.x) (&dsum[0][0][0])[k] = 0;
+                __syncthreads();
+                if (wp < 3)
+                    for (int w = 0; w < kWalkThreads / 32; w++) lk += lsum0[w][wp];
+            }
+            int buf = 0;
+            for (int e0 = L.e_begin; e0 < L.e_end; e0 += 32)
+            {
+                const int n = min(32, L.e_end - e0);
+                uint32_t m = 0, mp = 0;
+#pragma unroll 8
+                for (int j = 0; j < n; j++)
+                {
+                    bool wall;
+                    int ph;
+                    morton_step<W>(im.mi, sdir, P, seed, wall, ph);
+                    m = 2 * m + (wall ? 1u : 0u);
+                    if (NP == 2) mp = 2 * mp + ((wall && ph) ? 1u : 0u);
+                }
+                if (m)
+                {
+                    m <<= 32 - n; // echo j of the window at bit 31 - j
+                    mp <<= 32 - n;
+                    uint64_t eo = energy_fx<NP>(L.tfx, L.tstride, c);
+                    do
+                    {
+                        const int j = __clz(m);
+                        const uint32_t bit = 0x80000000u >> j;
+                        const uint32_t ph = (NP == 2 && (mp & bit)) ? 1u : 0u;
+                        m ^= bit;
+                        if (NP == 2)
+                        {
+                            c[0] += ph ^ 1u;
+                            c[1] += ph;
+                        }
+                        else
+                            c[0]++;
+                        const uint64_t en = energy_fx<NP>(L.tfx, L.tstride, c);
+                        uint32_t *d = dsum[buf][j];
+                        atomicAdd(d + 0, (uint32_t)(en & M21) - (uint32_t)(eo & M21));
+                        atomicAdd(d + 1, (uint32_t)((en >> 21) & M21) - (uint32_t)((eo >> 21) & M21));
+                        atomicAdd(d + 2, (uint32_t)(en >> 42) - (uint32_t)(eo >> 42));
+                        atomicAdd(d + 3, PACK ? 1u << (16 * ph) : 1u);
+                        eo = en;
+                    } while (m);
+                }
+                // every replay of this window is in dsum[buf]; the next window writes the other buffer,
+                // which the flush of the previous window emptied before this barrier
+                __syncthreads();
+                if (wp < 4)
+                {
+                    uint32_t v = dsum[buf][lane][wp];
+                    dsum[buf][lane][wp] = 0;
+                    unsigned long long *a = L.acc + (size_t)(e0 + 1 + lane) * K;
+                    if (wp < 3)
+                    {
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1)
+                        {
+                            const uint32_t t = __shfl_up_sync(FULL, v, o);
+                            if (lane >= o) v += t;
+                        }
+                        v += lk;
+                        lk = __shfl_sync(FULL, v, 31);
+                        if (lane < n && v) atomicAdd(a + wp, (unsigned long long)v);
+                    }
+                    else if (lane < n && v)
+                    {
+                        if (PACK)
+                        {
+                            if (v & 0xffffu) atomicAdd(a + 3, (unsigned long long)(v & 0xffffu));
+                            if (v >> 16) atomicAdd(a + 4, (unsigned long long)(v >> 16));
+                        }
+                        else
+                            atomicAdd(a + 3, (unsigned long long)v);
+                    }
+                }
+                buf ^= 1;
+            }
+        }
+    }
+    else if constexpr (FAST)
     {
         if (__syncthreads_and(active))
         {
