@@ -12,7 +12,10 @@
 //     (21/21/22 bits) and summed with warp-wide redux.sync, one lane per echo keeps the warp sum,
 //     warps combine in shared memory every 32 echoes and CTAs add into global 64-bit counters.
 //     Integer addition is associative, so results are bit-identical run to run and across launch
-//     shapes, and exact to 2^-63 per walker;
+//     shapes, and exact to 2^-63 per walker. At one step per echo (about 6 % of walkers collide
+//     per echo) the walk instead records each lane's collisions of a 32-echo window as bits and
+//     replays them after the window, adding the limb changes into per-echo shared counters: the
+//     same integers without a reduction per echo;
 //   * walker state is read once per launch and written once at its end; a launch covers a
 //     bounded number of echoes so that no single kernel runs for long on a shared GPU.
 #include <cstdint>
@@ -170,12 +173,14 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
             done = true;
             // One step per echo: during a window of n <= 32 echoes a lane only shifts its collisions
             // into bit masks (echo j of the window is bit n-1-j of m; the phase-1 ones also of mp).
-            // After the window each lane replays its few collisions in echo order and adds the change
-            // of its three energy limbs, and the collision, into the window's per-echo counters dsum
-            // (shared 32-bit atomics). The flush turns the changes into the CTA's limb sums after each
-            // echo with a prefix sum over the window, starting from the sums after the previous window.
-            // A CTA's limb sums stay below 2^30, so the 32-bit modular arithmetic is exact and the
-            // global counters receive the same integers as from per-echo warp reductions.
+            // After the window the warp replays its collisions, spread evenly over its lanes (walkers
+            // in narrow pores collide far more often than the average 2 per window), and adds each
+            // one's change of the walker's three energy limbs, and the collision, into the window's
+            // per-echo counters dsum (shared 32-bit atomics). The flush turns the changes into the
+            // CTA's limb sums after each echo with a prefix sum over the window, starting from the
+            // sums after the previous window. A CTA's limb sums stay below 2^30, so the 32-bit
+            // modular arithmetic is exact and the global counters receive the same integers as from
+            // per-echo warp reductions.
             __shared__ uint32_t dsum[2][32][4]; // [buffer][echo of the window][limb 0-2, collisions]
             __shared__ uint32_t lsum0[kWalkThreads / 32][3];
             const int wp = threadIdx.x >> 5;
@@ -210,33 +215,72 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                     m = 2 * m + (wall ? 1u : 0u);
                     if (NP == 2) mp = 2 * mp + ((wall && ph) ? 1u : 0u);
                 }
-                if (m)
+                // the warp's collisions of the window, spread evenly over its lanes: lane l takes
+                // collisions 32 r + l in (lane, echo) order; the owner lane and the collision's bit
+                // come from binary searches, its counts before and after from popcounts
+                m <<= 32 - n; // echo j of the window at bit 31 - j
+                mp <<= 32 - n;
+                const uint32_t kc = __popc(m);
+                uint32_t pre = kc; // inclusive prefix over lanes
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1)
                 {
-                    m <<= 32 - n; // echo j of the window at bit 31 - j
-                    mp <<= 32 - n;
-                    uint64_t eo = energy_fx<NP>(L.tfx, L.tstride, c);
-                    do
+                    const uint32_t t = __shfl_up_sync(FULL, pre, o);
+                    if (lane >= o) pre += t;
+                }
+                const uint32_t total = __shfl_sync(FULL, pre, 31);
+                pre -= kc; // exclusive
+                for (uint32_t base = 0; base < total; base += 32)
+                {
+                    const uint32_t ix = base + lane;
+                    int o = 0; // the last lane whose first collision index is <= ix
+#pragma unroll
+                    for (int st2 = 16; st2 >= 1; st2 >>= 1)
+                        if (__shfl_sync(FULL, pre, o + st2) <= ix) o += st2;
+                    const uint32_t mo = __shfl_sync(FULL, m, o);
+                    const uint32_t mpo = NP == 2 ? __shfl_sync(FULL, mp, o) : 0u;
+                    const uint32_t c0o = __shfl_sync(FULL, c[0], o);
+                    const uint32_t c1o = NP == 2 ? __shfl_sync(FULL, c[NP - 1], o) : 0u;
+                    const uint32_t q = ix - __shfl_sync(FULL, pre, o); // collisions of lane o before this one
+                    if (ix < total)
                     {
-                        const int j = __clz(m);
-                        const uint32_t bit = 0x80000000u >> j;
-                        const uint32_t ph = (NP == 2 && (mp & bit)) ? 1u : 0u;
-                        m ^= bit;
+                        int b = 0; // bit of the collision: the last b with more than q bits of mo at >= b
+#pragma unroll
+                        for (int st2 = 16; st2 >= 1; st2 >>= 1)
+                            if ((uint32_t)__popc(mo >> (b + st2)) > q) b += st2;
+                        const int jj = 31 - b;
+                        uint64_t eo, en;
+                        uint32_t ph = 0;
                         if (NP == 2)
                         {
-                            c[0] += ph ^ 1u;
-                            c[1] += ph;
+                            const uint32_t n1 = __popc((mpo >> b) >> 1); // phase-1 collisions before
+                            ph = (mpo >> b) & 1u;
+                            const uint32_t ca = c0o + (q - n1), cb = c1o + n1; // counts before
+                            const uint64_t ta = __ldg(L.tfx + ca), tb = __ldg(L.tfx + L.tstride + cb);
+                            const uint64_t tx = __ldg(L.tfx + (ph ? (size_t)L.tstride + cb + 1 : (size_t)ca + 1));
+                            eo = fx_mul(ta, tb);
+                            en = ph ? fx_mul(ta, tx) : fx_mul(tx, tb);
                         }
                         else
-                            c[0]++;
-                        const uint64_t en = energy_fx<NP>(L.tfx, L.tstride, c);
-                        uint32_t *d = dsum[buf][j];
+                        {
+                            eo = __ldg(L.tfx + c0o + q);
+                            en = __ldg(L.tfx + c0o + q + 1);
+                        }
+                        uint32_t *d = dsum[buf][jj];
                         atomicAdd(d + 0, (uint32_t)(en & M21) - (uint32_t)(eo & M21));
                         atomicAdd(d + 1, (uint32_t)((en >> 21) & M21) - (uint32_t)((eo >> 21) & M21));
                         atomicAdd(d + 2, (uint32_t)(en >> 42) - (uint32_t)(eo >> 42));
                         atomicAdd(d + 3, PACK ? 1u << (16 * ph) : 1u);
-                        eo = en;
-                    } while (m);
+                    }
                 }
+                if (NP == 2)
+                {
+                    const uint32_t k1 = __popc(mp);
+                    c[0] += kc - k1;
+                    c[1] += k1;
+                }
+                else
+                    c[0] += kc;
                 // every replay of this window is in dsum[buf]; the next window writes the other buffer,
                 // which the flush of the previous window emptied before this barrier
                 __syncthreads();
