@@ -12,10 +12,10 @@
 //     (21/21/22 bits) and summed with warp-wide redux.sync, one lane per echo keeps the warp sum,
 //     warps combine in shared memory every 32 echoes and CTAs add into global 64-bit counters.
 //     Integer addition is associative, so results are bit-identical run to run and across launch
-//     shapes, and exact to 2^-63 per walker. At one step per echo (about 6 % of walkers collide
-//     per echo) the walk instead records each lane's collisions of a 32-echo window as bits and
-//     replays them after the window, adding the limb changes into per-echo shared counters: the
-//     same integers without a reduction per echo;
+//     shapes, and exact to 2^-63 per walker. At one or two steps per echo (about 6 % of walkers
+//     collide per step) the walk instead records each lane's collisions of a 32-step window as
+//     bits and replays them after the window, adding the limb changes into per-echo shared
+//     counters: the same integers without a reduction per echo;
 //   * walker state is read once per launch and written once at its end; a launch covers a
 //     bounded number of echoes so that no single kernel runs for long on a shared GPU.
 #include <cstdint>
@@ -58,12 +58,16 @@ __device__ __forceinline__ void load_pos(const WalkState &s, int64_t i, WalkerPo
 // repeated product f_w * f_w * ..., one multiply per collision as in Walker::walk_3D, applied after
 // each echo for the collisions the echo gained and rounded to the same 2^63 fixed point.
 // Occupancy: at 256 threads, 8 resident blocks per SM need <= 32 registers a thread, 6 need <= 40,
-// 5 need <= 48. The minimum-block bounds below were chosen by measurement (+4 % two-phase, +6 %
-// one-phase walker-steps/s over the unbounded build); a few instances spill up to 16 bytes.
-template <int BC, int NP, bool PACK, bool WF, bool SENS = false>
+// 5 need <= 48. The minimum-block bounds below were chosen by measurement: 8 blocks for the bit-block
+// walks (+4 % two-phase, +6 % one-phase walker-steps/s over the unbounded build; a few instances spill
+// up to 16 bytes); for the Morton walks 5 blocks (48 registers; the collision replay 3.77e11 -> 4.34e11
+// on the two-phase 400^3 walk, the mapping walk +6.7 %), 6 for the three-step fast echo loop (+13 %),
+// where 32 registers spilled 70-140 bytes.
+template <int BC, int NP, bool PACK, bool WF, bool SENS = false, int SPE = 0, bool MORTON = false>
 constexpr int cpmg_min_blocks()
 {
     if (SENS) return NP == 4 ? 5 : 6; // the sensitivity sums need more than 32 registers
+    if (MORTON && !WF && (NP == 1 || PACK)) return SPE == 3 ? 6 : 5;
     return NP == 4 ? 5 : ((BC == BC_NOFLUX || BC == BC_GENERIC) && !WF && (NP == 1 || PACK) ? 8 : 6);
 }
 
@@ -75,7 +79,7 @@ constexpr int cpmg_min_blocks()
 // 2^-63 fixed-point energy times its collision count with phase q -- the forward sensitivities,
 // d(echo sum)/d f_q = sum E c_q / f_q. Each 96-bit product is summed as four 24-bit limbs.
 template <int BC, int NP, bool PACK, bool WF, int SPE, bool MORTON = false, bool SENS = false>
-__global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, WF, SENS>()))
+__global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, WF, SENS, SPE, MORTON>()))
     cpmg_walk_kernel(DevImage im, WalkState st, CpmgLaunch L)
 {
     static_assert(!PACK || NP == 2, "packed collision counts are for two phases");
@@ -164,15 +168,18 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
     // -- scattered over the lanes' counts late in a walk -- to a few lanes per warp (looking up every
     // lane every echo measured 25 % slower).
     constexpr bool FAST = MORTON && SPE > 0 && !SENS && !WF;
-    constexpr bool REPLAY = FAST && SPE == 1 && (NP == 1 || PACK);
+    // the collision replay for one or two steps per echo (at three the fast loop below measured faster:
+    // its per-echo work is already shared by three steps, and a window holds only 10 echoes)
+    constexpr bool REPLAY = FAST && SPE <= 2 && (NP == 1 || PACK);
+    constexpr int NE = SPE > 0 ? 32 / SPE : 1; // REPLAY: echoes per window (n SPE <= 32 steps)
     bool done = false;
     if constexpr (REPLAY)
     {
         if (__syncthreads_and(active))
         {
             done = true;
-            // One step per echo: during a window of n <= 32 echoes a lane only shifts its collisions
-            // into bit masks (echo j of the window is bit n-1-j of m; the phase-1 ones also of mp).
+            // During a window of n <= NE echoes (n SPE <= 32 steps) a lane only shifts its collisions
+            // into bit masks (step k of the window is bit n SPE - 1 - k of m; the phase-1 ones also of mp).
             // After the window the warp replays its collisions, spread evenly over its lanes (walkers
             // in narrow pores collide far more often than the average 2 per window), and adds each
             // one's change of the walker's three energy limbs, and the collision, into the window's
@@ -202,24 +209,28 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                     for (int w = 0; w < kWalkThreads / 32; w++) lk += lsum0[w][wp];
             }
             int buf = 0;
-            for (int e0 = L.e_begin; e0 < L.e_end; e0 += 32)
+            for (int e0 = L.e_begin; e0 < L.e_end; e0 += NE)
             {
-                const int n = min(32, L.e_end - e0);
+                const int n = min(NE, L.e_end - e0);
                 uint32_t m = 0, mp = 0;
-#pragma unroll 8
+#pragma unroll(SPE == 1 ? 8 : 4)
                 for (int j = 0; j < n; j++)
                 {
-                    bool wall;
-                    int ph;
-                    morton_step<W>(im.mi, sdir, P, seed, wall, ph);
-                    m = 2 * m + (wall ? 1u : 0u);
-                    if (NP == 2) mp = 2 * mp + ((wall && ph) ? 1u : 0u);
+#pragma unroll
+                    for (int s = 0; s < SPE; s++)
+                    {
+                        bool wall;
+                        int ph;
+                        morton_step<W>(im.mi, sdir, P, seed, wall, ph);
+                        m = 2 * m + (wall ? 1u : 0u);
+                        if (NP == 2) mp = 2 * mp + ((wall && ph) ? 1u : 0u);
+                    }
                 }
                 // the warp's collisions of the window, spread evenly over its lanes: lane l takes
                 // collisions 32 r + l in (lane, echo) order; the owner lane and the collision's bit
                 // come from binary searches, its counts before and after from popcounts
-                m <<= 32 - n; // echo j of the window at bit 31 - j
-                mp <<= 32 - n;
+                m <<= 32 - n * SPE; // step k of the window at bit 31 - k
+                mp <<= 32 - n * SPE;
                 const uint32_t kc = __popc(m);
                 uint32_t pre = kc; // inclusive prefix over lanes
 #pragma unroll
@@ -248,7 +259,7 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
 #pragma unroll
                         for (int st2 = 16; st2 >= 1; st2 >>= 1)
                             if ((uint32_t)__popc(mo >> (b + st2)) > q) b += st2;
-                        const int jj = 31 - b;
+                        const int jj = SPE == 1 ? 31 - b : (31 - b) / SPE; // the collision's echo
                         uint64_t eo, en;
                         uint32_t ph = 0;
                         if (NP == 2)

@@ -320,3 +320,17 @@ def test_cpmg_fixed_step_instances(engine, oracle, bc, spe, n_phases):
     w = walkers(lab, 2600, 21)
     g, st, o = run_both(engine, oracle, lab, w, 70, spe, dfactor([7.0, 30.0][:n_phases]), bc=bc, n_phases=n_phases)
     assert_parity(g, st, o)
+
+
+@pytest.mark.parametrize("chunk", [45, 64, 1000])
+@pytest.mark.parametrize("spe", [1, 2])
+@pytest.mark.parametrize("n_phases", [1, 2])
+def test_cpmg_collision_replay_across_launches(engine, oracle, chunk, spe, n_phases):
+    """The collision replay (one or two steps per echo, Morton walk) split into launches of 45, 64 and
+    1000 echoes: windows start at odd echoes, the last window of a launch is partial, and the counts
+    and per-CTA limb sums restart from the stored walker state at each launch."""
+    lab = image(shape=(40, 36, 44), n_phases=n_phases, seed=23)
+    w = walkers(lab, 5000, 29)
+    g, st, o = run_both(engine, oracle, lab, w, 230, spe, dfactor([12.0, 40.0][:n_phases]), n_phases=n_phases,
+                        chunk=chunk)
+    assert_parity(g, st, o)
