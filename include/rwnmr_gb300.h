@@ -82,7 +82,9 @@ double rwnmr_ctx_last_kernel_ms(const rwnmr_ctx *ctx);
 /* Bit-block image (BitBlock/bitBlock.cpp:138-221): blocks[bx + by*bcols + bz*bcols*brows],
  * bit (x%4) + 4*(y%4) + 16*(z%4) set for solid voxels, bcols = ceil(nx/4) etc.
  * labels (nullable): uint8 [nz][ny][nx], 0 = pore, p = solid of material phase p (1..n_phases);
- * must agree with blocks. Multi-phase labels extend the reference (its image is binary). */
+ * must agree with blocks. Multi-phase labels extend the reference (its image is binary). With
+ * n_phases > 1 a label above n_phases is rejected (RWNMR_ERR_INVALID); with n_phases = 1 every
+ * non-zero label is solid. */
 rwnmr_status rwnmr_image_upload(rwnmr_ctx *ctx, const uint64_t *blocks, int32_t nx, int32_t ny, int32_t nz,
                                 const uint8_t *labels, int32_t n_phases);
 /* Same from a label volume alone; the bit-blocks are packed on the GPU. */

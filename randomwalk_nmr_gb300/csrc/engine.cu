@@ -449,8 +449,8 @@ rwnmr_status rwnmr_image_upload_labels(rwnmr_ctx *c, const uint8_t *labels, int3
     RW_CUDA(c, c->blocks.ensure((size_t)nb * c->words), "image blocks");
     RW_CUDA(c, cudaMemcpyAsync(c->labels.p, labels, nvox, cudaMemcpyHostToDevice, c->stream), "labels upload");
     RW_CUDA(c, cudaMemsetAsync(c->status.p, 0, sizeof(unsigned), c->stream), "status reset");
-    RW_CUDA(c, launch_pack_blocks(c->labels.p, nx, ny, nz, c->bcols, c->brows, nb, c->words, c->blocks.p, c->status.p,
-                                  c->stream), "pack kernel");
+    RW_CUDA(c, launch_pack_blocks(c->labels.p, nx, ny, nz, c->bcols, c->brows, nb, c->words, c->n_phases, c->blocks.p,
+                                  c->status.p, c->stream), "pack kernel");
     c->launches++;
     RW_TRY(c->check_status("image packing"));
     if (c->n_phases == 1) c->labels.release();

@@ -34,6 +34,18 @@ namespace
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint64_t M21 = (1ull << 21) - 1;
 
+// The 96-bit product e * cq as four 24-bit limbs (the last holds bits 72-95).
+__device__ __forceinline__ void product_limbs24(uint64_t e, uint32_t cq, uint32_t *l)
+{
+    constexpr uint32_t M24 = (1u << 24) - 1;
+    const uint64_t lo = e * (uint64_t)cq;                     // bits 0-63
+    const uint32_t hi = (uint32_t)__umul64hi(e, (uint64_t)cq); // bits 64-95
+    l[0] = (uint32_t)lo & M24;
+    l[1] = (uint32_t)(lo >> 24) & M24;
+    l[2] = ((uint32_t)(lo >> 48) | (hi << 16)) & M24;
+    l[3] = hi >> 8;
+}
+
 // 2^63 fixed point of an energy in [0, 1]: round(e * 2^63), the rounding of the energy tables.
 __device__ __forceinline__ uint64_t walker_fx(double e) { return __double2ull_rn(e * 0x1p63); }
 
@@ -66,7 +78,9 @@ __device__ __forceinline__ void load_pos(const WalkState &s, int64_t i, WalkerPo
 template <int BC, int NP, bool PACK, bool WF, bool SENS = false, int SPE = 0, bool MORTON = false>
 constexpr int cpmg_min_blocks()
 {
-    if (SENS) return NP == 4 ? 5 : 6; // the sensitivity sums need more than 32 registers
+    // the sensitivity sums need more than 32 registers; their collision replay (one or two steps per
+    // echo) at four phases 64 (48 spilled 68 bytes: 35.7 vs 33.5 ms per 4-phase 200^3 walk)
+    if (SENS) return NP == 4 ? (MORTON && SPE >= 1 && SPE <= 2 ? 4 : 5) : 6;
     if (MORTON && !WF && (NP == 1 || PACK)) return SPE == 3 ? 6 : 5;
     return NP == 4 ? 5 : ((BC == BC_NOFLUX || BC == BC_GENERIC) && !WF && (NP == 1 || PACK) ? 8 : 6);
 }
@@ -168,10 +182,15 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
     // -- scattered over the lanes' counts late in a walk -- to a few lanes per warp (looking up every
     // lane every echo measured 25 % slower).
     constexpr bool FAST = MORTON && SPE > 0 && !SENS && !WF;
-    // the collision replay for one or two steps per echo (at three the fast loop below measured faster:
-    // its per-echo work is already shared by three steps, and a window holds only 10 echoes)
-    constexpr bool REPLAY = FAST && SPE <= 2 && (NP == 1 || PACK);
-    constexpr int NE = SPE > 0 ? 32 / SPE : 1; // REPLAY: echoes per window (n SPE <= 32 steps)
+    // the collision replay at one or two steps per echo, for the plain and the sensitivity walks (at
+    // three the per-echo work is shared by three steps: the fast loop below measured faster for the plain
+    // walk, and the per-echo reductions as fast for the sensitivity walk)
+    constexpr bool REPLAY = MORTON && SPE > 0 && SPE <= 2 && !WF && (SENS || NP == 1 || PACK);
+    constexpr int NE = SPE > 0 ? 32 / SPE : 1;          // REPLAY: echoes per window (n SPE <= 32 steps)
+    constexpr int NB = NP == 1 ? 0 : (NP == 2 ? 1 : 2); // REPLAY: phase bit-planes of a window's collisions
+    constexpr int KC = PACK ? 4 : K;                    // REPLAY: per-echo counters (PACK: one count word)
+    constexpr int NW = kWalkThreads / 32;
+    constexpr int KF = (KC + NW - 1) / NW; // counters flushed per warp
     bool done = false;
     if constexpr (REPLAY)
     {
@@ -179,40 +198,60 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
         {
             done = true;
             // During a window of n <= NE echoes (n SPE <= 32 steps) a lane only shifts its collisions
-            // into bit masks (step k of the window is bit n SPE - 1 - k of m; the phase-1 ones also of mp).
-            // After the window the warp replays its collisions, spread evenly over its lanes (walkers
-            // in narrow pores collide far more often than the average 2 per window), and adds each
-            // one's change of the walker's three energy limbs, and the collision, into the window's
-            // per-echo counters dsum (shared 32-bit atomics). The flush turns the changes into the
-            // CTA's limb sums after each echo with a prefix sum over the window, starting from the
-            // sums after the previous window. A CTA's limb sums stay below 2^30, so the 32-bit
-            // modular arithmetic is exact and the global counters receive the same integers as from
-            // per-echo warp reductions.
-            __shared__ uint32_t dsum[2][32][4]; // [buffer][echo of the window][limb 0-2, collisions]
-            __shared__ uint32_t lsum0[kWalkThreads / 32][3];
+            // into bit masks: step k of the window is bit n SPE - 1 - k of m, and of mb[0..NB) the bits of
+            // the colliding phase. After the window the warp replays its collisions, spread evenly over
+            // its lanes (walkers in narrow pores collide far more often than the average 2 per window),
+            // and adds each one's change of the walker's three energy limbs (SENS: and of the four
+            // limbs of each E c_q), and the collision, into the window's per-echo counters dsum (shared
+            // 32-bit atomics). The flush turns the changes into the CTA's sums after each echo with a
+            // prefix sum over the window, starting from the sums after the previous window. A CTA's
+            // limb sums stay below 2^32 (256 lanes x 2^24), so the 32-bit modular arithmetic is exact
+            // and the global counters receive the same integers as from per-echo warp reductions.
+            __shared__ uint32_t dsum[2][32][KC]; // [buffer][echo of the window][counter]
+            __shared__ uint32_t lsum0[NW][3 + KS];
             const int wp = threadIdx.x >> 5;
-            uint32_t lk = 0; // warps 0-2: the CTA's sum of limb wp after the last flushed echo
+            // level counters (energy limbs; SENS: limbs of E c_q) carry the CTA's sums from window to
+            // window; the collision counters are per echo
+            auto is_level = [](int col) { return col < 3 || col >= 3 + NG; };
+            uint32_t lk[KF]; // the CTA's sums of this warp's level counters after the last flushed echo
             {
                 const uint64_t es = energy_fx<NP>(L.tfx, L.tstride, c);
-                const uint32_t r0 = __reduce_add_sync(FULL, (uint32_t)(es & M21));
-                const uint32_t r1 = __reduce_add_sync(FULL, (uint32_t)((es >> 21) & M21));
-                const uint32_t r2 = __reduce_add_sync(FULL, (uint32_t)(es >> 42));
-                if (lane == 0)
+                uint32_t r[3 + KS];
+                r[0] = __reduce_add_sync(FULL, (uint32_t)(es & M21));
+                r[1] = __reduce_add_sync(FULL, (uint32_t)((es >> 21) & M21));
+                r[2] = __reduce_add_sync(FULL, (uint32_t)(es >> 42));
+                if constexpr (SENS)
                 {
-                    lsum0[wp][0] = r0;
-                    lsum0[wp][1] = r1;
-                    lsum0[wp][2] = r2;
+#pragma unroll
+                    for (int q = 0; q < NP; q++)
+                    {
+                        uint32_t l[4];
+                        product_limbs24(es, c[q], l);
+#pragma unroll
+                        for (int k = 0; k < 4; k++) r[3 + 4 * q + k] = __reduce_add_sync(FULL, l[k]);
+                    }
                 }
-                for (int k = threadIdx.x; k < 2 * 32 * 4; k += blockDim.x) (&dsum[0][0][0])[k] = 0;
+                if (lane == 0)
+#pragma unroll
+                    for (int k = 0; k < 3 + KS; k++) lsum0[wp][k] = r[k];
+                for (int k = threadIdx.x; k < 2 * 32 * KC; k += blockDim.x) (&dsum[0][0][0])[k] = 0;
                 __syncthreads();
-                if (wp < 3)
-                    for (int w = 0; w < kWalkThreads / 32; w++) lk += lsum0[w][wp];
+#pragma unroll
+                for (int t = 0; t < KF; t++)
+                {
+                    const int col = wp + t * NW;
+                    lk[t] = 0;
+                    if (col < KC && is_level(col))
+                        for (int w = 0; w < NW; w++) lk[t] += lsum0[w][col < 3 ? col : col - NG];
+                }
             }
             int buf = 0;
             for (int e0 = L.e_begin; e0 < L.e_end; e0 += NE)
             {
                 const int n = min(NE, L.e_end - e0);
-                uint32_t m = 0, mp = 0;
+                uint32_t m = 0, mb[NB > 0 ? NB : 1];
+#pragma unroll
+                for (int k = 0; k < NB; k++) mb[k] = 0;
 #pragma unroll(SPE == 1 ? 8 : 4)
                 for (int j = 0; j < n; j++)
                 {
@@ -223,14 +262,16 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                         int ph;
                         morton_step<W>(im.mi, sdir, P, seed, wall, ph);
                         m = 2 * m + (wall ? 1u : 0u);
-                        if (NP == 2) mp = 2 * mp + ((wall && ph) ? 1u : 0u);
+#pragma unroll
+                        for (int k = 0; k < NB; k++) mb[k] = 2 * mb[k] + ((wall && ((ph >> k) & 1)) ? 1u : 0u);
                     }
                 }
                 // the warp's collisions of the window, spread evenly over its lanes: lane l takes
                 // collisions 32 r + l in (lane, echo) order; the owner lane and the collision's bit
                 // come from binary searches, its counts before and after from popcounts
                 m <<= 32 - n * SPE; // step k of the window at bit 31 - k
-                mp <<= 32 - n * SPE;
+#pragma unroll
+                for (int k = 0; k < NB; k++) mb[k] <<= 32 - n * SPE;
                 const uint32_t kc = __popc(m);
                 uint32_t pre = kc; // inclusive prefix over lanes
 #pragma unroll
@@ -249,78 +290,128 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                     for (int st2 = 16; st2 >= 1; st2 >>= 1)
                         if (__shfl_sync(FULL, pre, o + st2) <= ix) o += st2;
                     const uint32_t mo = __shfl_sync(FULL, m, o);
-                    const uint32_t mpo = NP == 2 ? __shfl_sync(FULL, mp, o) : 0u;
-                    const uint32_t c0o = __shfl_sync(FULL, c[0], o);
-                    const uint32_t c1o = NP == 2 ? __shfl_sync(FULL, c[NP - 1], o) : 0u;
-                    const uint32_t q = ix - __shfl_sync(FULL, pre, o); // collisions of lane o before this one
+                    uint32_t mbo[NB > 0 ? NB : 1], co[NP];
+#pragma unroll
+                    for (int k = 0; k < NB; k++) mbo[k] = __shfl_sync(FULL, mb[k], o);
+#pragma unroll
+                    for (int q = 0; q < NP; q++) co[q] = __shfl_sync(FULL, c[q], o);
+                    const uint32_t qr = ix - __shfl_sync(FULL, pre, o); // collisions of lane o before this one
                     if (ix < total)
                     {
-                        int b = 0; // bit of the collision: the last b with more than q bits of mo at >= b
+                        int b = 0; // bit of the collision: the last b with more than qr bits of mo at >= b
 #pragma unroll
                         for (int st2 = 16; st2 >= 1; st2 >>= 1)
-                            if ((uint32_t)__popc(mo >> (b + st2)) > q) b += st2;
+                            if ((uint32_t)__popc(mo >> (b + st2)) > qr) b += st2;
                         const int jj = SPE == 1 ? 31 - b : (31 - b) / SPE; // the collision's echo
-                        uint64_t eo, en;
-                        uint32_t ph = 0;
-                        if (NP == 2)
+                        // the collision's phase and the walker's counts before it
+                        uint32_t ph = 0, cb[NP];
+                        if constexpr (NB == 0)
+                            cb[0] = co[0] + qr;
+                        else if constexpr (NB == 1)
                         {
-                            const uint32_t n1 = __popc((mpo >> b) >> 1); // phase-1 collisions before
-                            ph = (mpo >> b) & 1u;
-                            const uint32_t ca = c0o + (q - n1), cb = c1o + n1; // counts before
-                            const uint64_t ta = __ldg(L.tfx + ca), tb = __ldg(L.tfx + L.tstride + cb);
-                            const uint64_t tx = __ldg(L.tfx + (ph ? (size_t)L.tstride + cb + 1 : (size_t)ca + 1));
-                            eo = fx_mul(ta, tb);
-                            en = ph ? fx_mul(ta, tx) : fx_mul(tx, tb);
+                            const uint32_t n1 = __popc((mbo[0] >> b) >> 1); // phase-1 collisions before
+                            ph = (mbo[0] >> b) & 1u;
+                            cb[0] = co[0] + (qr - n1);
+                            cb[1] = co[1] + n1;
                         }
                         else
                         {
-                            eo = __ldg(L.tfx + c0o + q);
-                            en = __ldg(L.tfx + c0o + q + 1);
+                            const uint32_t a0 = (mbo[0] >> b) >> 1, a1 = (mbo[1] >> b) >> 1;
+                            const uint32_t nq[4] = {0u, (uint32_t)__popc(a0 & ~a1), (uint32_t)__popc(a1 & ~a0),
+                                                    (uint32_t)__popc(a0 & a1)};
+                            ph = ((mbo[0] >> b) & 1u) | (((mbo[1] >> b) & 1u) << 1);
+                            cb[0] = co[0] + (qr - nq[1] - nq[2] - nq[3]);
+#pragma unroll
+                            for (int q = 1; q < NP; q++) cb[q] = co[q] + nq[q];
+                        }
+                        // energies before and after: the tables' product in energy_fx's order, the
+                        // colliding phase's entry advanced by one
+                        uint64_t t[NP];
+                        uint32_t cph = cb[0];
+#pragma unroll
+                        for (int q = 0; q < NP; q++)
+                        {
+                            t[q] = __ldg(L.tfx + (size_t)q * L.tstride + cb[q]);
+                            if (q > 0 && ph == (uint32_t)q) cph = cb[q];
+                        }
+                        const uint64_t tx = __ldg(L.tfx + (size_t)ph * L.tstride + cph + 1);
+                        uint64_t eo = t[0], en = ph == 0 ? tx : t[0];
+#pragma unroll
+                        for (int q = 1; q < NP; q++)
+                        {
+                            eo = fx_mul(eo, t[q]);
+                            en = fx_mul(en, ph == (uint32_t)q ? tx : t[q]);
                         }
                         uint32_t *d = dsum[buf][jj];
                         atomicAdd(d + 0, (uint32_t)(en & M21) - (uint32_t)(eo & M21));
                         atomicAdd(d + 1, (uint32_t)((en >> 21) & M21) - (uint32_t)((eo >> 21) & M21));
                         atomicAdd(d + 2, (uint32_t)(en >> 42) - (uint32_t)(eo >> 42));
-                        atomicAdd(d + 3, PACK ? 1u << (16 * ph) : 1u);
+                        if (PACK) atomicAdd(d + 3, 1u << (16 * ph));
+                        else atomicAdd(d + 3 + ph, 1u);
+                        if constexpr (SENS)
+                        {
+#pragma unroll
+                            for (int q = 0; q < NP; q++)
+                            {
+                                uint32_t lo4[4], ln4[4];
+                                product_limbs24(eo, cb[q], lo4);
+                                product_limbs24(en, cb[q] + (ph == (uint32_t)q ? 1u : 0u), ln4);
+#pragma unroll
+                                for (int k = 0; k < 4; k++) atomicAdd(d + 3 + NP + 4 * q + k, ln4[k] - lo4[k]);
+                            }
+                        }
                     }
                 }
-                if (NP == 2)
+                if constexpr (NB == 0)
+                    c[0] += kc;
+                else if constexpr (NB == 1)
                 {
-                    const uint32_t k1 = __popc(mp);
+                    const uint32_t k1 = __popc(mb[0]);
                     c[0] += kc - k1;
                     c[1] += k1;
                 }
                 else
-                    c[0] += kc;
+                {
+                    const uint32_t nq[4] = {0u, (uint32_t)__popc(mb[0] & ~mb[1]), (uint32_t)__popc(mb[1] & ~mb[0]),
+                                            (uint32_t)__popc(mb[0] & mb[1])};
+                    c[0] += kc - nq[1] - nq[2] - nq[3];
+#pragma unroll
+                    for (int q = 1; q < NP; q++) c[q] += nq[q];
+                }
                 // every replay of this window is in dsum[buf]; the next window writes the other buffer,
                 // which the flush of the previous window emptied before this barrier
                 __syncthreads();
-                if (wp < 4)
-                {
-                    uint32_t v = dsum[buf][lane][wp];
-                    dsum[buf][lane][wp] = 0;
-                    unsigned long long *a = L.acc + (size_t)(e0 + 1 + lane) * K;
-                    if (wp < 3)
-                    {
 #pragma unroll
-                        for (int o = 1; o < 32; o <<= 1)
-                        {
-                            const uint32_t t = __shfl_up_sync(FULL, v, o);
-                            if (lane >= o) v += t;
-                        }
-                        v += lk;
-                        lk = __shfl_sync(FULL, v, 31);
-                        if (lane < n && v) atomicAdd(a + wp, (unsigned long long)v);
-                    }
-                    else if (lane < n && v)
+                for (int t = 0; t < KF; t++)
+                {
+                    const int col = wp + t * NW; // warp-uniform
+                    if (col < KC)
                     {
-                        if (PACK)
+                        uint32_t v = dsum[buf][lane][col];
+                        dsum[buf][lane][col] = 0;
+                        unsigned long long *a = L.acc + (size_t)(e0 + 1 + lane) * K;
+                        if (is_level(col))
                         {
-                            if (v & 0xffffu) atomicAdd(a + 3, (unsigned long long)(v & 0xffffu));
-                            if (v >> 16) atomicAdd(a + 4, (unsigned long long)(v >> 16));
+#pragma unroll
+                            for (int o = 1; o < 32; o <<= 1)
+                            {
+                                const uint32_t u = __shfl_up_sync(FULL, v, o);
+                                if (lane >= o) v += u;
+                            }
+                            v += lk[t];
+                            lk[t] = __shfl_sync(FULL, v, 31);
+                            if (lane < n && v) atomicAdd(a + col, (unsigned long long)v);
                         }
-                        else
-                            atomicAdd(a + 3, (unsigned long long)v);
+                        else if (lane < n && v)
+                        {
+                            if (PACK)
+                            {
+                                if (v & 0xffffu) atomicAdd(a + 3, (unsigned long long)(v & 0xffffu));
+                                if (v >> 16) atomicAdd(a + 4, (unsigned long long)(v >> 16));
+                            }
+                            else
+                                atomicAdd(a + col, (unsigned long long)v);
+                        }
                     }
                 }
                 buf ^= 1;
@@ -938,7 +1029,8 @@ __global__ void __launch_bounds__(256) pfgse_direct_kernel(DirectLaunch L)
 // Packs a label volume into bit-blocks with phase planes (BitBlock/bitBlock.cpp:138-221 plus the
 // multi-phase extension). One thread per block; voxels beyond the image edge stay pore.
 __global__ void pack_blocks_kernel(const uint8_t *__restrict__ labels, int nx, int ny, int nz, int bcols, int brows,
-                                   int64_t nblocks, int words, uint64_t *__restrict__ out, unsigned *status)
+                                   int64_t nblocks, int words, int n_phases, uint64_t *__restrict__ out,
+                                   unsigned *status)
 {
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nblocks) return;
@@ -954,7 +1046,9 @@ __global__ void pack_blocks_kernel(const uint8_t *__restrict__ labels, int nx, i
         if (!l) continue;
         solid |= 1ull << k;
         const unsigned ph = (unsigned)l - 1u;
-        if (ph >= 8u) atomicOr(status, kStatusBadLabel);
+        // multi-phase images: a label must name one of the image's phases (single-phase images treat
+        // every non-zero label as solid)
+        if (ph >= 8u || (n_phases > 1 && ph >= (unsigned)n_phases)) atomicOr(status, kStatusBadLabel);
         p0 |= (uint64_t)(ph & 1u) << k;
         p1 |= (uint64_t)((ph >> 1) & 1u) << k;
         p2 |= (uint64_t)((ph >> 2) & 1u) << k;
@@ -1174,11 +1268,11 @@ cudaError_t launch_pfgse_direct(const DirectLaunch &L, int n_delta, int blocks, 
 }
 
 cudaError_t launch_pack_blocks(const uint8_t *labels, int nx, int ny, int nz, int bcols, int brows, int64_t nblocks,
-                               int words, uint64_t *out, unsigned *status, cudaStream_t s)
+                               int words, int n_phases, uint64_t *out, unsigned *status, cudaStream_t s)
 {
     const int t = 256;
     pack_blocks_kernel<<<(unsigned)((nblocks + t - 1) / t), t, 0, s>>>(labels, nx, ny, nz, bcols, brows, nblocks,
-                                                                       words, out, status);
+                                                                       words, n_phases, out, status);
     return cudaGetLastError();
 }
 

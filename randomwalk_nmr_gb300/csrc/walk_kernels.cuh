@@ -177,7 +177,8 @@ inline MortonImage morton_params(int nx, int ny, int nz, uint32_t &n_words, int 
 
 // Builds the Morton copy im.mi describes (n_words x W uint32) from im's bit-blocks.
 cudaError_t launch_morton_build(const DevImage &im, int W, uint32_t n_words, uint32_t *out, cudaStream_t s);
+// labels above n_phases (multi-phase images) set kStatusBadLabel
 cudaError_t launch_pack_blocks(const uint8_t *labels, int nx, int ny, int nz, int bcols, int brows, int64_t nblocks,
-                               int words, uint64_t *out, unsigned *status, cudaStream_t s);
+                               int words, int n_phases, uint64_t *out, unsigned *status, cudaStream_t s);
 
 } // namespace rwnmr

@@ -111,15 +111,19 @@ def _collision_histories(oracle, lab, w, n_echoes, spe, f, n_phases, bc):
     return counts
 
 
-@pytest.mark.parametrize("n_phases,morton,bc", [(1, True, "noflux"), (2, True, "noflux"), (4, True, "noflux"),
-                                                (2, False, "noflux"), (3, False, "periodic"), (1, False, "mirror")])
-def test_sensitivities_exact(engine, oracle, n_phases, morton, bc):
+@pytest.mark.parametrize("n_phases,morton,bc,spe", [(1, True, "noflux", 3), (2, True, "noflux", 3),
+                                                    (4, True, "noflux", 3), (3, True, "noflux", 1),
+                                                    (4, True, "noflux", 2), (2, True, "noflux", 1),
+                                                    (2, False, "noflux", 3), (3, False, "periodic", 3),
+                                                    (1, False, "mirror", 3)])
+def test_sensitivities_exact(engine, oracle, n_phases, morton, bc, spe):
     """rwnmr_cpmg_run_sens: the same echo train as rwnmr_cpmg_run, and per-echo sums of E * c_q that
     equal, exactly, the sums formed from the oracle's per-walker collision histories and the engine's
-    fixed-point tables; their gradient equals the seed-replay adjoint's."""
+    fixed-point tables; their gradient equals the seed-replay adjoint's. The Morton walk replays each
+    window's collisions (1, 2 or 3 steps per echo; launches of 32 echoes split the windows)."""
     lab, w = setup(engine, n_phases, n=1500, morton=morton)
     assert engine.morton_layout == morton
-    n_echoes, spe = 40, 3
+    n_echoes = 40
     f = dfactor([10.0, 30.0, 5.0, 60.0][:n_phases])
     out = engine.cpmg_sens(n_echoes, spe, f, bc=bc, echoes_per_launch=32)
     plain = engine.cpmg(n_echoes, spe, f, bc=bc)

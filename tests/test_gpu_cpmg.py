@@ -151,6 +151,20 @@ def test_cpmg_rejects_bad_input(engine):
         engine.cpmg(10, 1, 1.5)  # decrease factor outside [0, 1]
 
 
+@pytest.mark.parametrize("n_phases", [2, 3])
+def test_labels_beyond_the_phase_count_are_rejected(engine, n_phases):
+    """A multi-phase upload whose labels name a phase beyond n_phases fails (the walks index the
+    per-phase tables by the voxel's phase); single-phase images take any non-zero label as solid."""
+    from randomwalk_nmr_gb300 import RwnmrError
+
+    lab = image(n_phases=n_phases + 1)
+    assert lab.max() == n_phases + 1
+    with pytest.raises(RwnmrError, match="exceeds the phase count"):
+        engine.upload_labels(lab, n_phases)
+    engine.upload_labels(lab, n_phases + 1)
+    engine.upload_labels(lab, 1)
+
+
 @pytest.mark.parametrize("bc,n_phases", [("noflux", 1), ("periodic", 1), ("noflux", 2), ("mirror", 4)])
 def test_map_walk_matches_oracle(engine, oracle, bc, n_phases):
     lab = image(seed=4, n_phases=n_phases)
