@@ -357,8 +357,31 @@ __device__ __forceinline__ void walker_step(const DevImage &im, WalkerPos &p, ui
 // a move down), and the steps to subtract from the axis field f = P & m for the move and for its
 // reversal: in dilated arithmetic (f - m) & m is f + 1 and (f - 1) & m is f - 1. Kept in shared
 // memory, so that decoding a direction is one lookup instead of integer compares and selects.
-__host__ __device__ inline uint4 morton_direction(const MortonImage &mi, int r)
+// The Morton walks index this table by slot = 2 ((-a) mod 3) + (a mod 2) of the xorshift state a
+// (morton_dir_slot) instead of by r = a mod 6; slot s stands for the direction r with r = -(s >> 1)
+// (mod 3) and r = s (mod 2).
+__host__ __device__ inline int morton_slot_direction(int slot)
 {
+    const int r3 = (3 - (slot >> 1)) % 3;
+    return r3 + 3 * ((r3 ^ slot) & 1);
+}
+
+// Direction slot of the state a (see morton_slot_direction), the same draw as mod6 with the remainder
+// by 3 on the multiplier: the fold t = lo + hi (+ carry) keeps a mod 3 (2^32 = 1 mod 3), and for
+// t = 3k + r the product t * 0xAAAAAAAB (the inverse of 3 mod 2^32) is k + r * 0xAAAAAAAB mod 2^32,
+// which lies in [0, 0x55555555] for r = 0, in [0x55555556, 0xAAAAAAAA] for r = 2 and in
+// [0xAAAAAAAB, 2^32) for r = 1 (k <= 0x55555554 for r > 0): its high product by 3 is (-r) mod 3.
+__device__ __forceinline__ uint32_t morton_dir_slot(uint64_t a)
+{
+    const uint32_t lo = (uint32_t)a, hi = (uint32_t)(a >> 32);
+    uint32_t t = lo + hi;
+    t += (t < lo) ? 1u : 0u;
+    return 2u * __umulhi(t * 0xAAAAAAABu, 3u) + (lo & 1u);
+}
+
+__host__ __device__ inline uint4 morton_direction(const MortonImage &mi, int slot)
+{
+    const int r = morton_slot_direction(slot);
     const uint32_t m = r >= 4 ? mi.mz : ((r & 1) ? mi.mx : mi.my);
     const bool up = r == 2 || r == 3 || r == 4;
     const uint32_t edge = up ? (r >= 4 ? mi.ez : ((r & 1) ? mi.ex : mi.ey)) : 0u;
@@ -367,13 +390,13 @@ __host__ __device__ inline uint4 morton_direction(const MortonImage &mi, int r)
 
 // One noflux step on the Morton copy (see MortonImage): the same xorshift64 draw, direction and
 // reversal rule as walker_step<BC_NOFLUX>, with the position held as the Morton index P. dirs: the
-// six morton_direction entries.
+// six morton_direction entries, by slot.
 template <int W>
 __device__ __forceinline__ void morton_step(const MortonImage &mi, const uint4 *dirs, uint32_t &P, uint64_t &seed,
                                             bool &wall, int &phase)
 {
     seed = xorshift64(seed);
-    const uint4 d = dirs[mod6(seed)];
+    const uint4 d = dirs[morton_dir_slot(seed)];
     const uint32_t f = P & d.x;
     // a move off the image is reversed (walker.h:444-491): a move up at the last voxel goes down, a
     // move down at voxel 0 goes up (every axis has at least two voxels)
