@@ -263,7 +263,8 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                         morton_step<W>(im.mi, sdir, P, seed, wall, ph);
                         m = 2 * m + (wall ? 1u : 0u);
 #pragma unroll
-                        for (int k = 0; k < NB; k++) mb[k] = 2 * mb[k] + ((wall && ((ph >> k) & 1)) ? 1u : 0u);
+                        // a phase bit is set only at solid voxels, so it implies the collision
+                        for (int k = 0; k < NB; k++) mb[k] = 2 * mb[k] + ((uint32_t)ph >> k & 1u);
                     }
                 }
                 // the warp's collisions of the window, spread evenly over its lanes: lane l takes
@@ -438,7 +439,8 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                         bool wall;
                         int ph;
                         morton_step<W>(im.mi, sdir, P, seed, wall, ph);
-                        if (PACK) g[0] += (wall ? 1u : 0u) << (ph << 4);
+                        // Morton copy: a phase bit implies the collision, so phase 1 adds 1 + 0xffff
+                        if (PACK) g[0] += MORTON ? (wall ? 1u : 0u) + (uint32_t)ph * 0xffffu : (wall ? 1u : 0u) << (ph << 4);
                         else
                         {
 #pragma unroll
@@ -520,7 +522,8 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                             morton_step<W>(im.mi, sdir, P, seed, wall, ph);
                         else
                             walker_step<BC, W>(im, p, seed, wall, ph);
-                        if (PACK) g[0] += (wall ? 1u : 0u) << (ph << 4);
+                        // Morton copy: a phase bit implies the collision, so phase 1 adds 1 + 0xffff
+                        if (PACK) g[0] += MORTON ? (wall ? 1u : 0u) + (uint32_t)ph * 0xffffu : (wall ? 1u : 0u) << (ph << 4);
                         else
                         {
 #pragma unroll
@@ -1095,6 +1098,7 @@ __global__ void morton_build_kernel(DevImage im, int W, uint32_t n_words, uint32
                 acc[k] = r;
             }
         }
+        for (int k = 1; k < W; k++) acc[k] &= acc[0]; // phase bits only at solid voxels
         for (int k = 0; k < W; k++) out[(size_t)w * W + k] = acc[k];
         return;
     }
@@ -1108,6 +1112,7 @@ __global__ void morton_build_kernel(DevImage im, int W, uint32_t n_words, uint32
         const uint32_t *bp = base + (size_t)blk * (2 * W) + (bit >> 5) * W;
         for (int k = 0; k < W; k++) acc[k] |= ((bp[k] >> (bit & 31)) & 1u) << b;
     }
+    for (int k = 1; k < W; k++) acc[k] &= acc[0];
     for (int k = 0; k < W; k++) out[(size_t)w * W + k] = acc[k];
 }
 
