@@ -173,14 +173,15 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
     }
     __syncthreads();
 
-    // The Morton walk with a fixed step count per echo and per-phase tables (the benchmark's walk):
-    // when every walker of the CTA is live (every CTA but a partial last one, unless a walker started
-    // outside the image), a copy of the echo loop without the per-lane liveness branch, unrolled 8
-    // echoes deep at one step per echo (4 at two or three) so that the loop and window bookkeeping is
-    // shared (+5 % on the one-step-per-echo walk). The choice is CTA-uniform, so both loops reach the same barriers. The per-lane `changed`
-    // test stays: only lanes whose counts changed look up their energy, which keeps the table gathers
-    // -- scattered over the lanes' counts late in a walk -- to a few lanes per warp (looking up every
-    // lane every echo measured 25 % slower).
+    // The Morton walks with a fixed step count per echo and per-phase tables take, when every walker of
+    // the CTA is live (every CTA but a partial last one, unless a walker started outside the image), one
+    // of two loops without the per-lane liveness branch; the choice is CTA-uniform, so every loop reaches
+    // the same barriers. At one or two steps per echo (one phase, packed two phases, or the sensitivity
+    // walks) the collision replay below; otherwise the fast echo loop: the echo loop unrolled 8 echoes
+    // deep at one step per echo (4 at two or three) so that the loop and window bookkeeping is shared
+    // (+5 % on the one-step-per-echo walk before the replay). Its per-lane `changed` test stays: only
+    // lanes whose counts changed look up their energy, which keeps the table gathers -- scattered over
+    // the lanes' counts late in a walk -- to a few lanes per warp (every lane every echo: 25 % slower).
     constexpr bool FAST = MORTON && SPE > 0 && !SENS && !WF;
     // the collision replay at one or two steps per echo, for the plain and the sensitivity walks (at
     // three the per-echo work is shared by three steps: the fast loop below measured faster for the plain
