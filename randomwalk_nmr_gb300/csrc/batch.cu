@@ -400,6 +400,11 @@ __global__ void batch_range_kernel(BatchLaunch L, int n_images)
 // 2 (t % 16), 2 (t % 16) + 1 for the 4 echoes rg .. rg + 3, rg = 4 (t / 16) -- 16 multiply-adds per
 // count from one 16-byte load of its 4 counts and one of its 2 values. Histogram counts and candidate
 // values are staged through shared memory kEvChunk counts at a time.
+// acc += a * b (32 x 32 -> 64 bits) as one multiply-add with a 64-bit addend
+__device__ __forceinline__ void mad_wide(unsigned long long &acc, unsigned a, unsigned b)
+{
+    asm("mad.wide.u32 %0, %1, %2, %0;" : "+l"(acc) : "r"(a), "r"(b));
+}
 constexpr int kEvRows = 32, kEvChunk = 64, kEvThreads = 128;
 constexpr int kEvRowsPerThread = 4;
 
@@ -448,15 +453,16 @@ __global__ void __launch_bounds__(kEvThreads) batch_eval_kernel(BatchLaunch L, i
         }
         for (int k = threadIdx.x; k < kEvChunk * kCand / 2; k += kEvThreads)
         {
-            const int q = k / kEvChunk, cc = k % kEvChunk; // candidate pair q, count c0 + cc
+            // candidate pair q, count c0 + cc: consecutive threads take consecutive pairs, so that a
+            // warp's 16-byte stores fill whole rows of sv (no bank conflicts)
+            const int q = k % (kCand / 2), cc = k / (kCand / 2);
             const int64_t c = c0 + cc;
             ulonglong2 t = make_ulonglong2(0, 0), tm = make_ulonglong2(0, 0);
             if (c < L.tstride) t = tab2[(size_t)q * L.tstride + c];
             if (c >= 1 && c < L.tstride) tm = tab2[(size_t)q * L.tstride + c - 1];
-            sv[cc][2 * q] = t.x;
-            sv[cc][2 * q + 1] = t.y;
-            sv[cc][kCand + 2 * q] = (unsigned long long)c * (tm.x >> L.dshift);
-            sv[cc][kCand + 2 * q + 1] = (unsigned long long)c * (tm.y >> L.dshift);
+            *reinterpret_cast<ulonglong2 *>(&sv[cc][2 * q]) = t;
+            *reinterpret_cast<ulonglong2 *>(&sv[cc][kCand + 2 * q]) =
+                make_ulonglong2((unsigned long long)c * (tm.x >> L.dshift), (unsigned long long)c * (tm.y >> L.dshift));
         }
         __syncthreads();
 #pragma unroll 4
@@ -470,10 +476,10 @@ __global__ void __launch_bounds__(kEvThreads) batch_eval_kernel(BatchLaunch L, i
 #pragma unroll
             for (int k = 0; k < kEvRowsPerThread; k++)
             {
-                lo[k][0] += (unsigned long long)hv[k] * vl0;
-                hi[k][0] += (unsigned long long)hv[k] * vh0;
-                lo[k][1] += (unsigned long long)hv[k] * vl1;
-                hi[k][1] += (unsigned long long)hv[k] * vh1;
+                mad_wide(lo[k][0], hv[k], vl0);
+                mad_wide(hi[k][0], hv[k], vh0);
+                mad_wide(lo[k][1], hv[k], vl1);
+                mad_wide(hi[k][1], hv[k], vh1);
             }
         }
         __syncthreads();
