@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                 uint32_t m = 0, mb[NB > 0 ? NB : 1];
 #pragma unroll
                 for (int k = 0; k < NB; k++) mb[k] = 0;
-#pragma unroll(SPE == 1 ? 8 : 4)
+#pragma unroll(SPE == 1 ? (SENS ? 8 : 16) : 4)
                 for (int j = 0; j < n; j++)
                 {
 #pragma unroll
