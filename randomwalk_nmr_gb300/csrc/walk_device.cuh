@@ -6,9 +6,9 @@
 //   position -> image-space lookup -> bit test in the 4x4x4 bit-block -> move, or count a
 //   collision on the solid voxel's phase.
 // The formulation here is branch-free integer code:
-//   * mod 6 of the 64-bit state uses 2^32 = 1 (mod 3): a mod 3 = (hi + lo + carry) mod 3, and the
-//     parity of a picks r or r+3. This equals the reference's digit-sum mod6 (walker.h:566-582)
-//     for every 64-bit value.
+//   * the direction (the reference's digit-sum mod6 of the state, walker.h:566-582) is drawn as the
+//     slot 2 ((-a) mod 3) + (a mod 2) (dir_slot): the same six outcomes, one slot per direction, with
+//     the remainder by 3 on the multiplier.
 //   * periodic and mirror boundaries keep the image-space coordinate incrementally (wrap, or
 //     stay-and-flip the tile orientation) instead of the per-step modulo of
 //     NMR_cpmg_cuda.cpp:1991-2015; positions stay unwrapped like the reference's.
@@ -92,14 +92,18 @@ __device__ __forceinline__ uint64_t xorshift64(uint64_t x)
     return x;
 }
 
-// state mod 6, see the file comment.
-__device__ __forceinline__ uint32_t mod6(uint64_t a)
+// Direction slot of the xorshift state a: 2 ((-a) mod 3) + (a mod 2). The 32-bit fold t = lo + hi (+ carry)
+// keeps a mod 3 (2^32 = 1 mod 3), and for t = 3k + r the product t * 0xAAAAAAAB (the inverse of 3 mod 2^32)
+// is k + r * 0xAAAAAAAB mod 2^32, which lies in [0, 0x55555555] for r = 0, in [0x55555556, 0xAAAAAAAA] for
+// r = 2 and in [0xAAAAAAAB, 2^32) for r = 1 (k <= 0x55555554 for r > 0): its high product by 3 is (-r) mod 3.
+// Slot s stands for the direction a mod 6 = r6 with r6 = -(s >> 1) (mod 3) and r6 = s (mod 2):
+// 0:N(-y) 1:E(+x) 2:S(+y) 3:Down(-z) 4:Up(+z) 5:W(-x) (reference numbering 0:N 1:W 2:S 3:E 4:Up 5:Down).
+__device__ __forceinline__ uint32_t dir_slot(uint64_t a)
 {
-    uint32_t lo = (uint32_t)a, hi = (uint32_t)(a >> 32);
+    const uint32_t lo = (uint32_t)a, hi = (uint32_t)(a >> 32);
     uint32_t t = lo + hi;
-    t += (t < lo) ? 1u : 0u; // carry of lo + hi is worth 2^32 = 1 (mod 3)
-    uint32_t r3 = t % 3u;
-    return r3 + 3u * ((r3 ^ lo) & 1u);
+    t += (t < lo) ? 1u : 0u;
+    return 2u * __umulhi(t * 0xAAAAAAABu, 3u) + (lo & 1u);
 }
 
 // Reference periodic / mirror image index for the generic path (NMR_cpmg_cuda.cpp:1991-2015).
@@ -228,10 +232,10 @@ template <int BC, int W>
 __device__ __forceinline__ void walker_step(const DevImage &im, WalkerPos &p, uint64_t &seed, bool &wall, int &phase)
 {
     seed = xorshift64(seed);
-    const uint32_t r = mod6(seed); // 0:N(-y) 1:W(-x) 2:S(+y) 3:E(+x) 4:Up(+z) 5:Down(-z)
-    int dx = (r == 3u) - (r == 1u);
+    const uint32_t r = dir_slot(seed); // 0:N(-y) 1:E(+x) 2:S(+y) 3:Down(-z) 4:Up(+z) 5:W(-x)
+    int dx = (r == 1u) - (r == 5u);
     int dy = (r == 2u) - (r == 0u);
-    int dz = (r == 4u) - (r == 5u);
+    int dz = (r == 4u) - (r == 3u);
 
     int tx, ty, tz;    // candidate real position
     int cix, ciy, ciz; // candidate image position
@@ -357,26 +361,12 @@ __device__ __forceinline__ void walker_step(const DevImage &im, WalkerPos &p, ui
 // a move down), and the steps to subtract from the axis field f = P & m for the move and for its
 // reversal: in dilated arithmetic (f - m) & m is f + 1 and (f - 1) & m is f - 1. Kept in shared
 // memory, so that decoding a direction is one lookup instead of integer compares and selects.
-// The Morton walks index this table by slot = 2 ((-a) mod 3) + (a mod 2) of the xorshift state a
-// (morton_dir_slot) instead of by r = a mod 6; slot s stands for the direction r with r = -(s >> 1)
-// (mod 3) and r = s (mod 2).
+// The Morton walks index this table by the direction slot of the state (dir_slot); slot s stands for
+// the direction r with r = -(s >> 1) (mod 3) and r = s (mod 2).
 __host__ __device__ inline int morton_slot_direction(int slot)
 {
     const int r3 = (3 - (slot >> 1)) % 3;
     return r3 + 3 * ((r3 ^ slot) & 1);
-}
-
-// Direction slot of the state a (see morton_slot_direction), the same draw as mod6 with the remainder
-// by 3 on the multiplier: the fold t = lo + hi (+ carry) keeps a mod 3 (2^32 = 1 mod 3), and for
-// t = 3k + r the product t * 0xAAAAAAAB (the inverse of 3 mod 2^32) is k + r * 0xAAAAAAAB mod 2^32,
-// which lies in [0, 0x55555555] for r = 0, in [0x55555556, 0xAAAAAAAA] for r = 2 and in
-// [0xAAAAAAAB, 2^32) for r = 1 (k <= 0x55555554 for r > 0): its high product by 3 is (-r) mod 3.
-__device__ __forceinline__ uint32_t morton_dir_slot(uint64_t a)
-{
-    const uint32_t lo = (uint32_t)a, hi = (uint32_t)(a >> 32);
-    uint32_t t = lo + hi;
-    t += (t < lo) ? 1u : 0u;
-    return 2u * __umulhi(t * 0xAAAAAAABu, 3u) + (lo & 1u);
 }
 
 __host__ __device__ inline uint4 morton_direction(const MortonImage &mi, int slot)
@@ -396,7 +386,7 @@ __device__ __forceinline__ void morton_step(const MortonImage &mi, const uint4 *
                                             bool &wall, int &phase)
 {
     seed = xorshift64(seed);
-    const uint4 d = dirs[morton_dir_slot(seed)];
+    const uint4 d = dirs[dir_slot(seed)];
     const uint32_t f = P & d.x;
     // a move off the image is reversed (walker.h:444-491): a move up at the last voxel goes down, a
     // move down at voxel 0 goes up (every axis has at least two voxels)

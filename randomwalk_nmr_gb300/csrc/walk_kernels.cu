@@ -82,6 +82,7 @@ constexpr int cpmg_min_blocks()
     // echo) at four phases 64 (48 spilled 68 bytes: 35.7 vs 33.5 ms per 4-phase 200^3 walk)
     if (SENS) return NP == 4 ? (MORTON && SPE >= 1 && SPE <= 2 ? 4 : 5) : 6;
     if (MORTON && !WF && (NP == 1 || PACK)) return SPE == 3 ? 6 : 5;
+    if (SPE >= 1 && SPE <= 2 && !WF && (NP == 1 || PACK)) return 5; // the bit-block collision replay
     return NP == 4 ? 5 : ((BC == BC_NOFLUX || BC == BC_GENERIC) && !WF && (NP == 1 || PACK) ? 8 : 6);
 }
 
@@ -183,10 +184,10 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
     // lanes whose counts changed look up their energy, which keeps the table gathers -- scattered over
     // the lanes' counts late in a walk -- to a few lanes per warp (every lane every echo: 25 % slower).
     constexpr bool FAST = MORTON && SPE > 0 && !SENS && !WF;
-    // the collision replay at one or two steps per echo, for the plain and the sensitivity walks (at
-    // three the per-echo work is shared by three steps: the fast loop below measured faster for the plain
-    // walk, and the per-echo reductions as fast for the sensitivity walk)
-    constexpr bool REPLAY = MORTON && SPE > 0 && SPE <= 2 && !WF && (SENS || NP == 1 || PACK);
+    // the collision replay at one or two steps per echo, for the plain and the sensitivity walks, Morton
+    // or bit-block steps (at three the per-echo work is shared by three steps: the fast loop below
+    // measured faster for the plain walk, and the per-echo reductions as fast for the sensitivity walk)
+    constexpr bool REPLAY = SPE > 0 && SPE <= 2 && !WF && (SENS || NP == 1 || PACK);
     constexpr int NE = SPE > 0 ? 32 / SPE : 1;          // REPLAY: echoes per window (n SPE <= 32 steps)
     constexpr int NB = NP == 1 ? 0 : (NP == 2 ? 1 : 2); // REPLAY: phase bit-planes of a window's collisions
     constexpr int KC = PACK ? 4 : K;                    // REPLAY: per-echo counters (PACK: one count word)
@@ -261,11 +262,16 @@ __global__ void __launch_bounds__(kWalkThreads, (cpmg_min_blocks<BC, NP, PACK, W
                     {
                         bool wall;
                         int ph;
-                        morton_step<W>(im.mi, sdir, P, seed, wall, ph);
+                        if constexpr (MORTON)
+                            morton_step<W>(im.mi, sdir, P, seed, wall, ph);
+                        else
+                            walker_step<BC, W>(im, p, seed, wall, ph);
                         m = 2 * m + (wall ? 1u : 0u);
 #pragma unroll
-                        // a phase bit is set only at solid voxels, so it implies the collision
-                        for (int k = 0; k < NB; k++) mb[k] = 2 * mb[k] + ((uint32_t)ph >> k & 1u);
+                        // the Morton copy holds phase bits only at solid voxels, so there a phase bit
+                        // implies the collision; the bit-blocks may come from the caller
+                        for (int k = 0; k < NB; k++)
+                            mb[k] = 2 * mb[k] + ((MORTON || wall) ? ((uint32_t)ph >> k & 1u) : 0u);
                     }
                 }
                 // the warp's collisions of the window, spread evenly over its lanes: lane l takes

@@ -1,4 +1,4 @@
-"""The Morton walks' direction slot (walk_device.cuh: morton_dir_slot, morton_slot_direction) against
+"""The walks' direction slot (walk_device.cuh: dir_slot, morton_slot_direction) against
 the reference's direction draw, state mod 6 (Walker/walker.h:566-582): the fold of the 64-bit state
 keeps its residue mod 3, the product by the inverse of 3 mod 2^32 and the high product by 3 give
 (-t) mod 3, and each slot stands for exactly one direction. CPU restatement of the device arithmetic."""
@@ -47,3 +47,12 @@ def test_slot_is_the_mod6_direction():
 
 def test_slots_cover_each_direction_once():
     assert sorted(slot_direction(np.arange(6))) == [0, 1, 2, 3, 4, 5]
+
+
+def test_bit_block_step_moves_by_slot():
+    """walker_step's moves by slot (0:N(-y) 1:E(+x) 2:S(+y) 3:Down(-z) 4:Up(+z) 5:W(-x)) are the moves of the
+    reference's directions (walker_defs.h: 0:N(-y) 1:W(-x) 2:S(+y) 3:E(+x) 4:Up(+z) 5:Down(-z))."""
+    ref_move = {0: (0, -1, 0), 1: (-1, 0, 0), 2: (0, 1, 0), 3: (1, 0, 0), 4: (0, 0, 1), 5: (0, 0, -1)}
+    for s in range(6):
+        move = (int(s == 1) - int(s == 5), int(s == 2) - int(s == 0), int(s == 4) - int(s == 3))
+        assert move == ref_move[int(slot_direction(np.array([s]))[0])], s
